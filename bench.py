@@ -1,0 +1,324 @@
+#!/usr/bin/env python3
+"""Benchmark of the embedded-RK step loop on BRUSS2D-MIX (steps/s and %HBM).
+
+Workload: BRUSS2D-MIX on an N=2000 grid (n = 8,000,000 components), DOPRI5(4),
+tol 1e-6, t in [0, 0.5], alpha 2e-3, initial values of the problem module --
+the FP64 configuration the reference's solver is quoted on.  A "step" is one
+attempted RK step (accepted or rejected) over all n components.
+
+  value    steps/s with y resident in HBM, K steps timed with CUDA events on the
+           solver's stream (one persistent launch runs the K steps)
+  e2e      the same through the C ABI with host buffers: pinned y0 copied in,
+           K steps, y copied out, timed on the host clock
+  roofline algorithmic bytes (16 n per attempted step: read y, write y) over the
+           launch time, against the measured HBM copy bandwidth; the FP64
+           pipe, not HBM, bounds this kernel, so "fp64" reports its share too
+  cpu_baseline the oracle port (the reference's D step loop restated in C,
+           pthreads over every host core) on a bounded sample of the same steps
+
+--gpus N runs N independent replicas (the path does not shard); value is
+the sum over replicas (N K steps over the slowest replica's time).
+--impl reference times the reference's CPU algorithm (the oracle port, every
+host thread) on the same workload instead.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+GRID_N = 2000
+ALPHA = 2e-3
+TOL = 1e-6
+T0, TE = 0.0, 0.5
+L2_BYTES = 129e6
+FALLBACK_HBM_GBS = 6800.0
+# FP64 pipe throughput measured on this GB300 pool with independent DFMA
+# chains: 505 G instr/s (1.01 TFLOP/s counting an FMA as 2 flops).
+FP64_GOPS_MEASURED = 505.0
+# FP64 instructions per component-step of the DOPRI5(4) loop on BRUSS2D-MIX
+# (counted from the kernel: 7 right-hand sides of 9.5/7.5 FP64 ops per
+# component, 31 nonzero tableau products, the update and the error norm)
+FP64_OPS_PER_COMP = {"exact": 128.0, "fma": 85.0}
+
+
+def _peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling during the timed region (SM clock, throttle reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.tmp = None
+
+    def start(self):
+        try:
+            self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.tmp, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.tmp.flush()
+        with open(self.tmp.name) as f:
+            rows = [r.split(",") for r in f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.tmp.name)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                smax = float(r[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _init_pg(ws, backend):
+    import torch.distributed as dist
+    if ws > 1 and not dist.is_initialized():
+        dist.init_process_group(backend)
+    return dist if ws > 1 else None
+
+
+def _max_over_ranks(x, dist, device=None):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline_port(threads, target_s=12.0, max_steps=400):
+    """Time the oracle port (reference D loop in C, pthreads) on the full-size
+    problem: as many steps as fit in about target_s, at least 2."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import rk_oracle
+    y0 = rk_oracle.bruss_start(GRID_N)
+    t = time.perf_counter()
+    rk_oracle.solve(rk_oracle.BRUSS2D_MIX, y0, "DOPRI54", T0, TE, TOL, step_limit=1,
+                    grid_n=GRID_N, alpha=ALPHA, threads=threads)
+    one = time.perf_counter() - t
+    steps = int(max(2, min(max_steps, target_s / max(one, 1e-6))))
+    t = time.perf_counter()
+    _, st = rk_oracle.solve(rk_oracle.BRUSS2D_MIX, y0, "DOPRI54", T0, TE, TOL, step_limit=steps,
+                            grid_n=GRID_N, alpha=ALPHA, threads=threads)
+    dt = time.perf_counter() - t
+    done = st["steps_acc"] + st["steps_rej"]
+    return done / dt, done, dt
+
+
+def run_reference(args):
+    ws, rank, local = _dist()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    # each "step" of this arm is one RK step on the full problem; the sample is
+    # bounded so the whole run ends within a few minutes
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import rk_oracle
+    y0 = rk_oracle.bruss_start(GRID_N)
+    t = time.perf_counter()
+    rk_oracle.solve(rk_oracle.BRUSS2D_MIX, y0, "DOPRI54", T0, TE, TOL, step_limit=max(1, args.warmup),
+                    grid_n=GRID_N, alpha=ALPHA, threads=threads)
+    warm = time.perf_counter() - t
+    per = warm / max(1, args.warmup)
+    k = max(2, min(args.steps, int(150.0 / max(per, 1e-6))))
+    t = time.perf_counter()
+    _, st = rk_oracle.solve(rk_oracle.BRUSS2D_MIX, y0, "DOPRI54", T0, TE, TOL, step_limit=k,
+                            grid_n=GRID_N, alpha=ALPHA, threads=threads)
+    dt = time.perf_counter() - t
+    k = st["steps_acc"] + st["steps_rej"]
+    v = k / dt
+    line = {
+        "impl": "reference", "metric": "BRUSS2D-MIX N=2000 DOPRI54 steps/s", "value": v,
+        "unit": "steps/s", "n_gpus": args.gpus, "steps": k, "warmup": args.warmup,
+        "ms_per_step": 1e3 * dt / k, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (ode_start initial values)",
+        "config": {"workload": "bruss2d-mix N=2000 n=8e6 DOPRI54 tol=1e-6 t=[0,0.5]",
+                   "grid_n": GRID_N, "alpha": ALPHA, "method": "DOPRI54"},
+        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
+                         "sample": f"first {k} steps of the N=2000 solve, D step loop, {threads} pthreads"},
+        "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import ctypes
+
+    import torch
+
+    import rk_gb300 as rk
+
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    dist = _init_pg(ws, "nccl")
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    prob = rk.bruss2d_mix(GRID_N, ALPHA)
+    n = prob.n
+    y0 = rk.ode_start(prob)
+    y0_dev = torch.from_numpy(y0).to(dev)
+    torch.cuda.synchronize()
+
+    solver = rk.Solver(prob, method=args.method, precision=args.precision, device=local,
+                       stream=stream.cuda_stream)
+    # ---- device-resident timing -------------------------------------------
+    solver.begin(T0, TE, None, TOL, y0_device_ptr=y0_dev.data_ptr())
+    solver.advance(args.warmup)
+    solver.query()
+    launches0 = solver.launches
+    clocks = ClockSampler(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    solver.advance(args.steps)
+    ev1.record(stream)
+    ev1.synchronize()
+    clk = clocks.stop()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    st = solver.query()
+    launches = solver.launches - launches0
+    steps_done = st["steps_acc"] + st["steps_rej"] - args.warmup
+    ms = ev0.elapsed_time(ev1)
+    ms_max = _max_over_ranks(ms, dist, dev)
+    value = ws * steps_done / (ms_max * 1e-3)
+
+    # ---- end to end through the C ABI with host buffers -------------------
+    pinned_in = torch.from_numpy(y0).pin_memory()
+    pinned_out = torch.empty(n, dtype=torch.float64).pin_memory()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    lib = rk.load()
+    t = time.perf_counter()
+    rc = lib.rkcu_begin(solver._h, T0, TE, ctypes.c_void_p(pinned_in.data_ptr()), 0, TOL)
+    assert rc == 0, rc
+    solver.advance(args.steps)
+    rc = lib.rkcu_get_y(solver._h, ctypes.c_void_p(pinned_out.data_ptr()), 0)
+    assert rc == 0, rc
+    e2e_s = time.perf_counter() - t
+    st2 = solver.query()
+    e2e_steps = st2["steps_acc"] + st2["steps_rej"]
+    e2e_s = _max_over_ranks(e2e_s, dist, dev)
+    e2e_value = ws * e2e_steps / e2e_s
+    dev_bytes = solver.device_bytes
+    solver.close()
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+
+    peak, peak_kind = _peaks()
+    per_step_bytes = 16.0 * n
+    launch_s = ms * 1e-3 / max(1, launches)
+    achieved = per_step_bytes * steps_done / max(1, launches) / launch_s / 1e9
+    fp64_ops = FP64_OPS_PER_COMP["exact" if args.precision == "exact" else "fma"] * n * steps_done
+    fp64_achieved = fp64_ops / (ms * 1e-3) / 1e9
+    line = {
+        "metric": "BRUSS2D-MIX N=2000 DOPRI54 steps/s", "value": value, "unit": "steps/s",
+        "n_gpus": ws, "steps": steps_done, "warmup": args.warmup,
+        "ms_per_step": ms_max / max(1, steps_done), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (ode_start initial values of BRUSS2D-MIX)",
+        "config": {"workload": "bruss2d-mix N=2000 n=8e6 DOPRI54 tol=1e-6 t=[0,0.5]",
+                   "grid_n": GRID_N, "alpha": ALPHA, "method": args.method,
+                   "precision": args.precision, "parallelism": f"replicas{ws}",
+                   "l2": f"per-step working set {dev_bytes / 1e6:.0f} MB > {L2_BYTES / 1e6:.0f} MB L2, no flush"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
+                     "kernel": "plain_kernel (persistent, all stages of K steps)"},
+        "fp64_roofline": {"achieved": fp64_achieved, "peak": FP64_GOPS_MEASURED,
+                          "unit": "G FP64 instr/s", "frac": fp64_achieved / FP64_GOPS_MEASURED,
+                          "ops_per_component_step": FP64_OPS_PER_COMP["exact" if args.precision == "exact" else "fma"]},
+        "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": 8.0 * n / max(1, e2e_steps),
+                "d2h_bytes_per_step": 8.0 * n / max(1, e2e_steps),
+                "note": f"one C-ABI begin/advance/get_y of {e2e_steps} steps, pinned host y0 and y"},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "device_bytes": dev_bytes,
+    }
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        v, k, dt = cpu_baseline_port(threads)
+        line["cpu_baseline"] = {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
+                                "sample": f"first {k} steps of the same N=2000 solve ({dt:.1f} s), "
+                                          f"D step loop restated in C, {threads} pthreads"}
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--method", default="DOPRI54")
+    ap.add_argument("--precision", default="fma", choices=["exact", "fma"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,154 @@
+/*
+ * rkcu -- C ABI of the GB300 embedded Runge-Kutta step loop.
+ *
+ * The reference binds its hot path through plain C: the solver entry
+ *   void solver(double t0, double te, double *y0, double *y, double tol);
+ * (include/solver.h:47), the problem module of include/ode.h:29-36
+ * (ode_size, ode_start, ode_eval_comp, ode_eval_rng, ode_acc_dist) and the
+ * tableau constructors of type rk_method_t (include/methods.h:92-93,
+ * src/methods.c:62-724).  A CUDA solver variant placed in the reference tree
+ * (src/impl/cuda/<Variant>.c) calls the entry points below; nothing here
+ * takes or returns a torch type, and every entry point returns an int status
+ * (the reference's solver() is void and only asserts).
+ *
+ * All state lives on one GPU.  Calls on one rkcu_solver are not thread-safe
+ * (the reference's solver() is not re-entrant either: it uses the globals
+ * ode_size and threads, src/main.c:30-36).
+ */
+#ifndef RKCU_H_
+#define RKCU_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define RKCU_OK                0
+#define RKCU_ERR_INVALID      -1   /* bad argument or unsupported combination */
+#define RKCU_ERR_CUDA         -2   /* a CUDA runtime call failed (rkcu_last_cuda_error) */
+#define RKCU_ERR_NOMEM        -3   /* device or pinned allocation failed */
+#define RKCU_ERR_TIMEOUT      -4   /* a device-side wait reached its time limit */
+#define RKCU_ERR_STATE        -5   /* call out of order (e.g. advance before begin) */
+#define RKCU_ERR_NO_DEVICE    -6   /* no CUDA device, or not an sm_103 device */
+
+/* ---- problems (include/ode.h modules) ---------------------------------- */
+#define RKCU_PROBLEM_BRUSS2D_MIX  0   /* src/problems/bruss2d-mix.c */
+#define RKCU_PROBLEM_LV_PAIRS     1   /* src/problems/lv.c */
+#define RKCU_PROBLEM_LV_BANDED    2   /* banded Lotka-Volterra chain (no reference module) */
+
+/* ---- arithmetic -------------------------------------------------------- */
+#define RKCU_FP64_EXACT  0   /* reference evaluation order, no contraction: bit-identical
+                                to the reference except where CUDA pow() and glibc pow()
+                                differ in the last bit of the step-size factor */
+#define RKCU_FP64_FMA    1   /* FP64 with fused multiply-adds (fewer FP64 instructions) */
+#define RKCU_MIXED       2   /* FP32 stage vectors, FP64 state, update and error norm */
+
+/* ---- solver variants (src/impl/seq/D.c, src/impl/seq/PipeDls.c) ------- */
+#define RKCU_VARIANT_D           0   /* stage vectors w_1..w_{s-1}, dy, err in HBM */
+#define RKCU_VARIANT_LOWSTORAGE  1   /* PipeDls idea: reduced stage storage */
+
+typedef struct rkcu_solver rkcu_solver;
+
+/* Problem description; replaces the compile-time macros of include/config.h:30-44
+   (BRUSS_GRID_SIZE, BRUSS_ALPHA, LV_COUNT) and the global ode_size (ode.h:29). */
+typedef struct
+{
+  int problem;          /* RKCU_PROBLEM_* */
+  int n;                /* ode_size; for BRUSS2D-MIX must equal 2*grid_n*grid_n */
+  int grid_n;           /* BRUSS_GRID_SIZE (>= 2) */
+  double alpha;         /* BRUSS_ALPHA */
+  const double *lv_r;   /* banded LV: r[n] (host memory, copied by rkcu_create) */
+  const double *lv_a;   /* banded LV: a[n][5] for offsets -2..2 (host, copied) */
+} rkcu_problem;
+
+typedef struct
+{
+  int precision;        /* RKCU_FP64_EXACT (default), RKCU_FP64_FMA, RKCU_MIXED */
+  int variant;          /* RKCU_VARIANT_D (default) */
+  int step_limit;       /* STEP_LIMIT (config.h:71, tools.h:191-198); 0 = no limit */
+  int device;           /* CUDA device ordinal */
+  void *stream;         /* cudaStream_t to run on; NULL = a stream owned by the solver */
+  double wait_timeout_s;/* limit of every device-side wait; <= 0 selects 10 s */
+} rkcu_options;
+
+/* Progress of a solve: the counters of src/tools.c:62-79 plus the current t, h. */
+typedef struct
+{
+  int steps_acc;
+  int steps_rej;
+  double t;
+  double h;
+  int done;             /* t >= te, or the step limit was reached */
+  int step_limit_reached;
+} rkcu_stats;
+
+void rkcu_options_default(rkcu_options *opt);
+
+/* Create a solver for one problem on one device.  Allocates nothing large yet. */
+int rkcu_create(rkcu_solver **out, const rkcu_problem *prob, const rkcu_options *opt);
+int rkcu_destroy(rkcu_solver *s);
+
+/* Install a tableau exactly as an rk_method_t fills it (methods.h:31-42,92-93):
+   A given as `stages` row pointers, b, b_hat (the embedded weights, not yet
+   transformed; b - b_hat is formed here as seq/D.c:40-41 does), c, order. */
+int rkcu_set_method(rkcu_solver *s, double **A, const double *b, const double *b_hat,
+                    const double *c, int stages, int ord);
+/* Same, for the tableaux of src/methods.c by name: "HEUN2", "RK4", "SSPRK3",
+   "RKF23", "DOPRI54", "VERNER65", "DOPRI87". */
+int rkcu_set_method_by_name(rkcu_solver *s, const char *name);
+/* Read a built-in tableau: A row-major [stages*stages]; arrays need 16 entries.
+   Returns RKCU_ERR_INVALID for an unknown name.  HAS_EMB_SOL (methods.h:95-118)
+   is returned in *embedded. */
+int rkcu_builtin_method(const char *name, double *A, double *b, double *b_hat, double *c,
+                        int *stages, int *ord, int *embedded);
+
+/* Whole integration with host buffers: the solver() contract of
+   include/solver.h:47.  y0 and y are host arrays of n doubles (may alias).
+   Copies y0 in once and y out once; the step loop stays on the GPU. */
+int rkcu_solve(rkcu_solver *s, double t0, double te, const double *y0, double *y,
+               double tol, rkcu_stats *stats);
+
+/* Device-resident flow, for callers that keep y in HBM:
+   begin  -- set t=t0, h=initial_stepsize (src/tools.c:25-36), y=y0 (y0 is a host
+             pointer if y0_on_device == 0, else a device pointer)
+   advance-- enqueue up to max_steps attempted steps on the solver's stream (async);
+             the device stops by itself at te or at the step limit
+   query  -- wait for the stream, read the counters
+   get_y  -- copy the current y out (host or device destination) */
+int rkcu_begin(rkcu_solver *s, double t0, double te, const double *y0, int y0_on_device,
+               double tol);
+int rkcu_advance(rkcu_solver *s, int max_steps);
+int rkcu_query(rkcu_solver *s, rkcu_stats *stats);
+int rkcu_get_y(rkcu_solver *s, double *y, int y_on_device);
+
+/* The device stream the solver runs on (cudaStream_t), for event timing. */
+void *rkcu_stream(rkcu_solver *s);
+/* Number of kernels this solver has launched so far. */
+long long rkcu_launch_count(rkcu_solver *s);
+/* Bytes of device memory this solver holds. */
+long long rkcu_device_bytes(rkcu_solver *s);
+
+/* Problem-module entry points of include/ode.h:31-35, for one problem instance:
+   ode_start (host arithmetic, bruss2d-mix.c:35-60 / lv.c:43-62), and a
+   device evaluation of the right-hand side over components [i, j]
+   (ode_eval_rng semantics: f[i..j] written, global indexing) computed by the
+   same device evaluator the step loop uses, in exact arithmetic. */
+int rkcu_ode_start(const rkcu_problem *prob, double t, double *y0);
+int rkcu_ode_eval_rng(const rkcu_problem *prob, int i, int j, double t, const double *y,
+                      double *f);
+int rkcu_ode_acc_dist(const rkcu_problem *prob);
+
+/* Test hook: make every later launch of this solver wait at its first grid
+   barrier for `extra_arrivals` CTAs that do not exist, so the bounded device
+   wait runs out and the call reports RKCU_ERR_TIMEOUT.  0 switches it off.
+   It lets tests exercise the timeout path without faulting or hanging a GPU. */
+int rkcu_debug_inject_wait_timeout(rkcu_solver *s, int extra_arrivals);
+
+const char *rkcu_strerror(int status);
+const char *rkcu_last_cuda_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RKCU_H_ */

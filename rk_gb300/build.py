@@ -1,0 +1,86 @@
+"""Build the rkcu CUDA library (sm_103a) and the CPU oracle, in tree.
+
+    python -m rk_gb300.build            # librkcu.so + oracle
+    python -m rk_gb300.build --verbose  # also print -Xptxas -v resource usage
+
+Outputs (git-ignored): rk_gb300/_lib/librkcu.so, oracle/_build/librk_oracle.so,
+rk_gb300/_lib/cuda_bruss2d-mix_D (drop-in driver binary).
+Each translation unit is compiled in parallel with one -gencode, so a build
+takes well under a minute on the GPU host as well as here.
+"""
+import argparse
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(PKG)
+CSRC = os.path.join(PKG, "csrc")
+LIBDIR = os.path.join(PKG, "_lib")
+OBJDIR = os.path.join(PKG, "_build")
+INCLUDE = os.path.join(REPO, "include")
+
+CU_SOURCES = ["rkcu_api.cu", "rkcu_plain.cu", "rkcu_methods.cu"]
+GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
+
+
+def nvcc():
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(cand):
+        raise RuntimeError("nvcc not found")
+    return cand
+
+
+def _run(cmd):
+    p = subprocess.run(cmd, capture_output=True, text=True)
+    if p.returncode != 0:
+        raise RuntimeError("command failed:\n" + " ".join(cmd) + "\n" + p.stdout + p.stderr)
+    return p.stdout + p.stderr
+
+
+def build_cuda(verbose=False):
+    os.makedirs(LIBDIR, exist_ok=True)
+    os.makedirs(OBJDIR, exist_ok=True)
+    flags = [GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
+             "-I" + INCLUDE, "-I" + CSRC, "--expt-relaxed-constexpr"]
+    if verbose:
+        flags.append("-Xptxas=-v")
+    jobs = []
+    for src in CU_SOURCES:
+        obj = os.path.join(OBJDIR, src.replace(".cu", ".o"))
+        jobs.append((obj, [nvcc(), *flags, "-c", os.path.join(CSRC, src), "-o", obj]))
+    outs = []
+    with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        for out in ex.map(lambda j: _run(j[1]), jobs):
+            outs.append(out)
+    lib = os.path.join(LIBDIR, "librkcu.so")
+    tmp = lib + ".tmp"
+    _run([nvcc(), GENCODE, "-shared", "-o", tmp, *[j[0] for j in jobs], "-lcudart"])
+    os.replace(tmp, lib)
+    if verbose:
+        sys.stdout.write("".join(outs))
+    return lib
+
+
+def build_oracle():
+    _run(["make", "-s", "-C", os.path.join(REPO, "oracle"), "oracle"])
+    return os.path.join(REPO, "oracle", "_build", "librk_oracle.so")
+
+
+def build_all(verbose=False):
+    lib = build_cuda(verbose)
+    orc = build_oracle()
+    return lib, orc
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--verbose", action="store_true")
+    a = ap.parse_args()
+    print(build_all(a.verbose))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,465 @@
+// C ABI of the step loop (include/rkcu.h): solver objects, device buffers,
+// launches and the problem-module helpers.  Host code only; the kernels are in
+// rkcu_plain.cu.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+
+#include "rkcu.h"
+#include "rkcu_plain.cuh"
+
+using rkcu::DevState;
+using rkcu::kMaxStages;
+
+namespace {
+
+thread_local char g_cuda_err[256] = "";
+
+int cuda_fail(cudaError_t e, const char *what) {
+  std::snprintf(g_cuda_err, sizeof(g_cuda_err), "%s: %s", what, cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? RKCU_ERR_NOMEM : RKCU_ERR_CUDA;
+}
+
+#define RKCU_CK(call)                                  \
+  do {                                                 \
+    cudaError_t e_ = (call);                           \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+size_t pairs_of(int n) { return (static_cast<size_t>(n) + 1) / 2; }
+
+int check_problem(const rkcu_problem *p) {
+  if (!p || p->n <= 0) return RKCU_ERR_INVALID;
+  switch (p->problem) {
+    case RKCU_PROBLEM_BRUSS2D_MIX:
+      if (p->grid_n < 2 || static_cast<long long>(p->n) != 2LL * p->grid_n * p->grid_n)
+        return RKCU_ERR_INVALID;
+      return RKCU_OK;
+    case RKCU_PROBLEM_LV_PAIRS:
+      return (p->n % 2 == 0) ? RKCU_OK : RKCU_ERR_INVALID;
+    case RKCU_PROBLEM_LV_BANDED:
+      return (p->lv_r && p->lv_a) ? RKCU_OK : RKCU_ERR_INVALID;
+    default:
+      return RKCU_ERR_INVALID;
+  }
+}
+
+// (alpha * (N-1)) * (N-1): the association of "BRUSS_ALPHA * N1 * N1" in
+// src/problems/bruss2d-mix.c:84
+double bruss_coef(const rkcu_problem *p) {
+  const double n1 = static_cast<double>(p->grid_n) - 1.0;
+  return p->alpha * n1 * n1;
+}
+
+}  // namespace
+
+struct rkcu_solver {
+  rkcu_problem prob{};
+  rkcu_options opt{};
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  // tableau
+  bool have_method = false;
+  int s = 0, ord = 0;
+  double A[kMaxStages * kMaxStages] = {};
+  double b[kMaxStages] = {}, bh[kMaxStages] = {};
+  // device memory
+  size_t npairs = 0;
+  double2 *y[2] = {nullptr, nullptr};
+  double2 *stage = nullptr;  // w[1..s-1], dy, err
+  int stage_vectors = 0;
+  double *lv_r = nullptr, *lv_a = nullptr;
+  DevState *st = nullptr;
+  DevState *st_host = nullptr;  // pinned
+  // run
+  bool begun = false;
+  double te = 0.0, tol = 0.0;
+  long long launches = 0;
+  long long dev_bytes = 0;
+  int last_grid = 0;
+  int extra_arrivals = 0;
+};
+
+extern "C" {
+
+void rkcu_options_default(rkcu_options *o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->precision = RKCU_FP64_EXACT;
+  o->variant = RKCU_VARIANT_D;
+  o->step_limit = 0;
+  o->device = 0;
+  o->stream = nullptr;
+  o->wait_timeout_s = 10.0;
+}
+
+const char *rkcu_strerror(int status) {
+  switch (status) {
+    case RKCU_OK: return "ok";
+    case RKCU_ERR_INVALID: return "invalid argument";
+    case RKCU_ERR_CUDA: return "CUDA error";
+    case RKCU_ERR_NOMEM: return "out of memory";
+    case RKCU_ERR_TIMEOUT: return "device wait timed out";
+    case RKCU_ERR_STATE: return "call out of order";
+    case RKCU_ERR_NO_DEVICE: return "no usable CUDA device";
+    default: return "unknown status";
+  }
+}
+
+const char *rkcu_last_cuda_error(void) { return g_cuda_err; }
+
+int rkcu_destroy(rkcu_solver *s) {
+  if (!s) return RKCU_ERR_INVALID;
+  cudaSetDevice(s->opt.device);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  cudaFree(s->y[0]);
+  cudaFree(s->y[1]);
+  cudaFree(s->stage);
+  cudaFree(s->lv_r);
+  cudaFree(s->lv_a);
+  cudaFree(s->st);
+  cudaFreeHost(s->st_host);
+  if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+  return RKCU_OK;
+}
+
+int rkcu_create(rkcu_solver **out, const rkcu_problem *prob, const rkcu_options *opt) {
+  if (!out) return RKCU_ERR_INVALID;
+  *out = nullptr;
+  int rc = check_problem(prob);
+  if (rc != RKCU_OK) return rc;
+  rkcu_options o;
+  if (opt)
+    o = *opt;
+  else
+    rkcu_options_default(&o);
+  if (o.precision != RKCU_FP64_EXACT && o.precision != RKCU_FP64_FMA) return RKCU_ERR_INVALID;
+  if (o.variant != RKCU_VARIANT_D) return RKCU_ERR_INVALID;
+  if (o.step_limit < 0) return RKCU_ERR_INVALID;
+  if (!(o.wait_timeout_s > 0.0)) o.wait_timeout_s = 10.0;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= o.device || o.device < 0)
+    return RKCU_ERR_NO_DEVICE;
+
+  rkcu_solver *s = new (std::nothrow) rkcu_solver();
+  if (!s) return RKCU_ERR_NOMEM;
+  s->prob = *prob;
+  s->prob.lv_r = s->prob.lv_a = nullptr;
+  s->opt = o;
+  s->npairs = pairs_of(prob->n);
+  auto fail = [&](int code) {
+    rkcu_destroy(s);
+    return code;
+  };
+  cudaError_t e;
+  if ((e = cudaSetDevice(o.device)) != cudaSuccess) return fail(cuda_fail(e, "cudaSetDevice"));
+  if ((e = cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, o.device)) !=
+      cudaSuccess)
+    return fail(cuda_fail(e, "cudaDeviceGetAttribute"));
+  if (o.stream) {
+    s->stream = static_cast<cudaStream_t>(o.stream);
+  } else {
+    if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess)
+      return fail(cuda_fail(e, "cudaStreamCreate"));
+    s->own_stream = true;
+  }
+  const size_t ybytes = s->npairs * sizeof(double2);
+  for (int k = 0; k < 2; ++k) {
+    if ((e = cudaMalloc(&s->y[k], ybytes)) != cudaSuccess) return fail(cuda_fail(e, "cudaMalloc y"));
+    if ((e = cudaMemset(s->y[k], 0, ybytes)) != cudaSuccess) return fail(cuda_fail(e, "cudaMemset"));
+    s->dev_bytes += ybytes;
+  }
+  if ((e = cudaMalloc(&s->st, sizeof(DevState))) != cudaSuccess)
+    return fail(cuda_fail(e, "cudaMalloc state"));
+  if ((e = cudaMallocHost(&s->st_host, sizeof(DevState))) != cudaSuccess)
+    return fail(cuda_fail(e, "cudaMallocHost"));
+  if (prob->problem == RKCU_PROBLEM_LV_BANDED) {
+    const size_t np = 2 * s->npairs;
+    if ((e = cudaMalloc(&s->lv_r, np * sizeof(double))) != cudaSuccess)
+      return fail(cuda_fail(e, "cudaMalloc r"));
+    if ((e = cudaMalloc(&s->lv_a, 5 * np * sizeof(double))) != cudaSuccess)
+      return fail(cuda_fail(e, "cudaMalloc a"));
+    cudaMemset(s->lv_r, 0, np * sizeof(double));
+    cudaMemset(s->lv_a, 0, 5 * np * sizeof(double));
+    if ((e = cudaMemcpy(s->lv_r, prob->lv_r, prob->n * sizeof(double), cudaMemcpyHostToDevice)) !=
+        cudaSuccess)
+      return fail(cuda_fail(e, "cudaMemcpy r"));
+    if ((e = cudaMemcpy(s->lv_a, prob->lv_a, 5 * (size_t)prob->n * sizeof(double),
+                        cudaMemcpyHostToDevice)) != cudaSuccess)
+      return fail(cuda_fail(e, "cudaMemcpy a"));
+    s->dev_bytes += 6 * np * sizeof(double);
+  }
+  *out = s;
+  return RKCU_OK;
+}
+
+int rkcu_set_method(rkcu_solver *s, double **A, const double *b, const double *b_hat,
+                    const double *c, int stages, int ord) {
+  (void)c;  // BRUSS2D-MIX and LV are autonomous: c only enters through t + h*c_i
+  if (!s || !A || !b || !b_hat || stages < 2 || stages > kMaxStages || ord < 1)
+    return RKCU_ERR_INVALID;
+  std::memset(s->A, 0, sizeof(s->A));
+  std::memset(s->b, 0, sizeof(s->b));
+  std::memset(s->bh, 0, sizeof(s->bh));
+  for (int i = 0; i < stages; ++i) {
+    if (!A[i]) return RKCU_ERR_INVALID;
+    for (int j = 0; j < i; ++j) s->A[i * kMaxStages + j] = A[i][j];
+    s->b[i] = b[i];
+    s->bh[i] = b[i] - b_hat[i];  // src/impl/seq/D.c:40-41
+  }
+  s->s = stages;
+  s->ord = ord;
+  s->have_method = true;
+  s->begun = false;
+  return RKCU_OK;
+}
+
+int rkcu_set_method_by_name(rkcu_solver *s, const char *name) {
+  if (!s) return RKCU_ERR_INVALID;
+  double A[kMaxStages * kMaxStages], b[16], bh[16], c[16];
+  int st = 0, ord = 0, emb = 0;
+  int rc = rkcu_builtin_method(name, A, b, bh, c, &st, &ord, &emb);
+  if (rc != RKCU_OK) return rc;
+  double *rows[kMaxStages];
+  for (int i = 0; i < st; ++i) rows[i] = A + i * st;
+  return rkcu_set_method(s, rows, b, bh, c, st, ord);
+}
+
+int rkcu_begin(rkcu_solver *s, double t0, double te, const double *y0, int y0_on_device,
+               double tol) {
+  if (!s || !y0 || !s->have_method) return s ? RKCU_ERR_STATE : RKCU_ERR_INVALID;
+  if (!(te == te) || !(t0 == t0)) return RKCU_ERR_INVALID;
+  if (tol <= 0.0 && s->opt.step_limit <= 0) return RKCU_ERR_INVALID;  // fixed step needs a limit
+  RKCU_CK(cudaSetDevice(s->opt.device));
+  const int need = s->s + 1;  // w[1..s-1], dy, err
+  if (s->stage_vectors < need) {
+    if (s->stage) {
+      RKCU_CK(cudaStreamSynchronize(s->stream));
+      cudaFree(s->stage);
+      s->dev_bytes -= (long long)s->stage_vectors * s->npairs * sizeof(double2);
+      s->stage = nullptr;
+      s->stage_vectors = 0;
+    }
+    RKCU_CK(cudaMalloc(&s->stage, (size_t)need * s->npairs * sizeof(double2)));
+    s->stage_vectors = need;
+    s->dev_bytes += (long long)need * s->npairs * sizeof(double2);
+  }
+  const size_t nbytes = (size_t)s->prob.n * sizeof(double);
+  if (s->prob.n % 2) RKCU_CK(cudaMemsetAsync(s->y[0], 0, s->npairs * sizeof(double2), s->stream));
+  RKCU_CK(cudaMemcpyAsync(s->y[0], y0, nbytes,
+                          y0_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                          s->stream));
+  // src/tools.c:25-36 (H_INIT unset): h = min(10 tol, H / STEP_LIMIT); STEP_LIMIT 0 gives H/0
+  const double H = te - t0;
+  const double lim = H / static_cast<double>(s->opt.step_limit);  // 0 gives +inf as in the reference
+  const double h0 = tol > 0.0 ? std::fmin(10.0 * tol, lim) : lim;
+  DevState *h = s->st_host;
+  std::memset(h, 0, sizeof(*h));
+  h->t = t0;
+  h->h = h0;
+  h->cur = 0;
+  h->done = !(t0 < te) || (s->opt.step_limit > 0 && 0 >= s->opt.step_limit);
+  RKCU_CK(cudaMemcpyAsync(s->st, h, sizeof(DevState), cudaMemcpyHostToDevice, s->stream));
+  RKCU_CK(cudaStreamSynchronize(s->stream));
+  s->te = te;
+  s->tol = tol;
+  s->begun = true;
+  return RKCU_OK;
+}
+
+int rkcu_advance(rkcu_solver *s, int max_steps) {
+  if (!s) return RKCU_ERR_INVALID;
+  if (!s->begun) return RKCU_ERR_STATE;
+  if (max_steps <= 0) return RKCU_OK;
+  RKCU_CK(cudaSetDevice(s->opt.device));
+  rkcu::PlainParams p;
+  std::memset(&p, 0, sizeof(p));
+  p.npairs = (int)s->npairs;
+  p.n = s->prob.n;
+  p.s = s->s;
+  p.ord = s->ord;
+  p.problem = s->prob.problem;
+  p.step_limit = s->opt.step_limit;
+  p.budget = max_steps;
+  p.te = s->te;
+  p.tol = s->tol;
+  p.timeout_ns = (unsigned long long)(s->opt.wait_timeout_s * 1e9);
+  for (int i = 0; i < kMaxStages * kMaxStages; ++i) {
+    p.A[i] = s->A[i];
+    p.nzA[i] = s->A[i] != 0.0;
+  }
+  for (int i = 0; i < kMaxStages; ++i) {
+    p.b[i] = s->b[i];
+    p.bh[i] = s->bh[i];
+    p.nzb[i] = s->b[i] != 0.0;
+    p.nzbh[i] = s->bh[i] != 0.0;
+  }
+  p.y[0] = s->y[0];
+  p.y[1] = s->y[1];
+  for (int l = 1; l < s->s; ++l) p.w[l] = s->stage + (size_t)(l - 1) * s->npairs;
+  p.dy = s->stage + (size_t)(s->s - 1) * s->npairs;
+  p.err = s->stage + (size_t)s->s * s->npairs;
+  p.st = s->st;
+  p.bruss.N = s->prob.grid_n;
+  p.bruss.coef = s->prob.problem == RKCU_PROBLEM_BRUSS2D_MIX ? bruss_coef(&s->prob) : 0.0;
+  p.lvb.n = s->prob.n;
+  p.lvb.r = s->lv_r;
+  p.lvb.a = s->lv_a;
+  p.extra_arrivals = s->extra_arrivals;
+  int grid = 0;
+  cudaError_t e = rkcu::launch_plain(p, s->opt.precision == RKCU_FP64_EXACT, 0, s->num_sms,
+                                     s->stream, &grid);
+  if (e != cudaSuccess) return cuda_fail(e, "plain kernel launch");
+  s->last_grid = grid;
+  ++s->launches;
+  return RKCU_OK;
+}
+
+int rkcu_query(rkcu_solver *s, rkcu_stats *stats) {
+  if (!s) return RKCU_ERR_INVALID;
+  if (!s->begun) return RKCU_ERR_STATE;
+  RKCU_CK(cudaSetDevice(s->opt.device));
+  RKCU_CK(cudaMemcpyAsync(s->st_host, s->st, sizeof(DevState), cudaMemcpyDeviceToHost, s->stream));
+  RKCU_CK(cudaStreamSynchronize(s->stream));
+  const DevState *h = s->st_host;
+  if (stats) {
+    stats->steps_acc = h->steps_acc;
+    stats->steps_rej = h->steps_rej;
+    stats->t = h->t;
+    stats->h = h->h;
+    stats->done = h->done;
+    stats->step_limit_reached =
+        s->opt.step_limit > 0 && h->steps_acc + h->steps_rej >= s->opt.step_limit;
+  }
+  if (h->error) {
+    std::snprintf(g_cuda_err, sizeof(g_cuda_err), "device wait timed out at site %d",
+                  h->error_site);
+    return RKCU_ERR_TIMEOUT;
+  }
+  return RKCU_OK;
+}
+
+int rkcu_get_y(rkcu_solver *s, double *y, int y_on_device) {
+  if (!s || !y) return RKCU_ERR_INVALID;
+  if (!s->begun) return RKCU_ERR_STATE;
+  RKCU_CK(cudaSetDevice(s->opt.device));
+  RKCU_CK(cudaMemcpyAsync(s->st_host, s->st, sizeof(DevState), cudaMemcpyDeviceToHost, s->stream));
+  RKCU_CK(cudaStreamSynchronize(s->stream));
+  const int cur = s->st_host->cur & 1;
+  RKCU_CK(cudaMemcpyAsync(y, s->y[cur], (size_t)s->prob.n * sizeof(double),
+                          y_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                          s->stream));
+  RKCU_CK(cudaStreamSynchronize(s->stream));
+  return RKCU_OK;
+}
+
+int rkcu_solve(rkcu_solver *s, double t0, double te, const double *y0, double *y, double tol,
+               rkcu_stats *stats) {
+  if (!s || !y0 || !y) return RKCU_ERR_INVALID;
+  int rc = rkcu_begin(s, t0, te, y0, 0, tol);
+  if (rc != RKCU_OK) return rc;
+  rkcu_stats st{};
+  for (;;) {
+    if ((rc = rkcu_advance(s, 1 << 16)) != RKCU_OK) return rc;
+    if ((rc = rkcu_query(s, &st)) != RKCU_OK) return rc;
+    if (st.done) break;
+  }
+  if ((rc = rkcu_get_y(s, y, 0)) != RKCU_OK) return rc;
+  if (stats) *stats = st;
+  return RKCU_OK;
+}
+
+int rkcu_debug_inject_wait_timeout(rkcu_solver *s, int extra_arrivals) {
+  if (!s || extra_arrivals < 0) return RKCU_ERR_INVALID;
+  s->extra_arrivals = extra_arrivals;
+  return RKCU_OK;
+}
+
+void *rkcu_stream(rkcu_solver *s) { return s ? (void *)s->stream : nullptr; }
+long long rkcu_launch_count(rkcu_solver *s) { return s ? s->launches : -1; }
+long long rkcu_device_bytes(rkcu_solver *s) { return s ? s->dev_bytes : -1; }
+
+int rkcu_ode_acc_dist(const rkcu_problem *prob) {
+  if (check_problem(prob) != RKCU_OK) return RKCU_ERR_INVALID;
+  switch (prob->problem) {
+    case RKCU_PROBLEM_BRUSS2D_MIX: return 2 * prob->grid_n;  // bruss2d-mix.c:718-721
+    case RKCU_PROBLEM_LV_PAIRS: return 1;                    // lv.c:127-130
+    default: return 2;                                       // band half-width
+  }
+}
+
+int rkcu_ode_start(const rkcu_problem *prob, double t, double *y0) {
+  (void)t;
+  if (!y0 || check_problem(prob) != RKCU_OK) return RKCU_ERR_INVALID;
+  if (prob->problem == RKCU_PROBLEM_BRUSS2D_MIX) {  // bruss2d-mix.c:51-59
+    const int N = prob->grid_n;
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < N; ++j) {
+        y0[2 * N * i + 2 * j] = 0.5 + (double)j / (double)(N - 1);
+        y0[2 * N * i + 2 * j + 1] = 1.0 + (5.0 * (double)i) / (double)(N - 1);
+      }
+    return RKCU_OK;
+  }
+  if (prob->problem == RKCU_PROBLEM_LV_PAIRS) {  // lv.c:56-60
+    for (int i = 0; i + 1 < prob->n; i += 2) {
+      y0[i] = 0.2;
+      y0[i + 1] = 1.1;
+    }
+    return RKCU_OK;
+  }
+  return RKCU_ERR_INVALID;  // the banded chain's initial values are given by the caller
+}
+
+int rkcu_ode_eval_rng(const rkcu_problem *prob, int i, int j, double t, const double *y,
+                      double *f) {
+  (void)t;
+  if (!y || !f || check_problem(prob) != RKCU_OK || i < 0 || j >= prob->n) return RKCU_ERR_INVALID;
+  if (j < i) return RKCU_OK;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return RKCU_ERR_NO_DEVICE;
+  const size_t np = pairs_of(prob->n);
+  double2 *dy = nullptr, *df = nullptr;
+  double *r = nullptr, *a = nullptr;
+  int rc = RKCU_OK;
+  cudaError_t e = cudaSuccess;
+  rkcu::Bruss br{prob->grid_n, prob->problem == RKCU_PROBLEM_BRUSS2D_MIX ? bruss_coef(prob) : 0.0};
+  rkcu::LvBanded lvb{prob->n, nullptr, nullptr};
+  if ((e = cudaMalloc(&dy, np * sizeof(double2))) != cudaSuccess) goto done;
+  if ((e = cudaMalloc(&df, np * sizeof(double2))) != cudaSuccess) goto done;
+  if ((e = cudaMemset(dy, 0, np * sizeof(double2))) != cudaSuccess) goto done;
+  if ((e = cudaMemcpy(dy, y, prob->n * sizeof(double), cudaMemcpyHostToDevice)) != cudaSuccess)
+    goto done;
+  if (prob->problem == RKCU_PROBLEM_LV_BANDED) {
+    if ((e = cudaMalloc(&r, 2 * np * sizeof(double))) != cudaSuccess) goto done;
+    if ((e = cudaMalloc(&a, 10 * np * sizeof(double))) != cudaSuccess) goto done;
+    cudaMemset(r, 0, 2 * np * sizeof(double));
+    cudaMemset(a, 0, 10 * np * sizeof(double));
+    if ((e = cudaMemcpy(r, prob->lv_r, prob->n * sizeof(double), cudaMemcpyHostToDevice)) !=
+        cudaSuccess)
+      goto done;
+    if ((e = cudaMemcpy(a, prob->lv_a, 5 * (size_t)prob->n * sizeof(double),
+                        cudaMemcpyHostToDevice)) != cudaSuccess)
+      goto done;
+    lvb.r = r;
+    lvb.a = a;
+  }
+  if ((e = rkcu::launch_eval_rhs(prob->problem, br, lvb, (int)np, dy, df, 0)) != cudaSuccess)
+    goto done;
+  if ((e = cudaDeviceSynchronize()) != cudaSuccess) goto done;
+  // ode_eval_rng writes f[i..j] with global indexing (ode.h:34, block-inline.h:338)
+  e = cudaMemcpy(f + i, reinterpret_cast<double *>(df) + i, (size_t)(j - i + 1) * sizeof(double),
+                 cudaMemcpyDeviceToHost);
+done:
+  if (e != cudaSuccess) rc = cuda_fail(e, "rkcu_ode_eval_rng");
+  cudaFree(dy);
+  cudaFree(df);
+  cudaFree(r);
+  cudaFree(a);
+  return rc;
+}
+
+}  // extern "C"

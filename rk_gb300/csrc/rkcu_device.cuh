@@ -1,0 +1,208 @@
+// Device building blocks shared by the rkcu kernels: arithmetic policies, the
+// right-hand sides of the problem modules, and a bounded grid barrier.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace rkcu {
+
+constexpr int kMaxStages = 13;   // DOPRI87 (src/methods.c:476) is the largest tableau
+
+// ---------------------------------------------------------------------------
+// Arithmetic policies.
+//
+// Exact: every product and sum is rounded once, in the order the reference's C
+// expressions imply, with explicit round-to-nearest intrinsics so that nvcc
+// cannot contract them into FMAs.  The two FMAs it does use, fma(-4,y,s) and
+// fma(2,y,s), are exact rewrites: 4y and 2y are exact in binary floating point,
+// so fma(-4,y,s) == s - 4.0*y rounded once, as in the reference.
+// Fused: contracts a*b+c into one FMA (fewer FP64 instructions).
+// ---------------------------------------------------------------------------
+template <bool kExact>
+struct Arith;
+
+template <>
+struct Arith<true> {
+  static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+  static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+  static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+  // acc + a*b with the product rounded first (C semantics without contraction)
+  static __device__ __forceinline__ double mac(double acc, double a, double b) {
+    return __dadd_rn(acc, __dmul_rn(a, b));
+  }
+  // a*b - c with the product rounded first
+  static __device__ __forceinline__ double msub(double a, double b, double c) {
+    return __dsub_rn(__dmul_rn(a, b), c);
+  }
+};
+
+template <>
+struct Arith<false> {
+  static __device__ __forceinline__ double mul(double a, double b) { return a * b; }
+  static __device__ __forceinline__ double add(double a, double b) { return a + b; }
+  static __device__ __forceinline__ double sub(double a, double b) { return a - b; }
+  static __device__ __forceinline__ double mac(double acc, double a, double b) { return fma(a, b, acc); }
+  static __device__ __forceinline__ double msub(double a, double b, double c) { return fma(a, b, -c); }
+};
+
+// ---------------------------------------------------------------------------
+// Right-hand sides.  The unit of work is a pair of consecutive components
+// (2p, 2p+1): one grid point (u, v) of BRUSS2D-MIX, one prey/predator pair of
+// LV, two neighbours of the banded chain.  Every vector is padded to an even
+// length, so a pair is one 16-byte aligned double2.
+// ---------------------------------------------------------------------------
+
+// BRUSS2D-MIX (src/problems/bruss2d-mix.c:66-206), grid point p = k*N + j.
+//   U: 1 + u^2 v - 4.4 u + alpha (N-1)^2 (sum of the 4 neighbours - 4u)
+//   V: 3.4 u - u^2 v     + alpha (N-1)^2 (sum of the 4 neighbours - 4v)
+// A missing neighbour at the boundary is replaced by the opposite one.  The
+// reference sums "yN + yS" first (a boundary row doubles the inner neighbour,
+// which "y + y" reproduces exactly), then adds W and E left to right in
+// interior columns, or "2 * inner" in one rounding in the first/last column.
+struct Bruss {
+  int N;        // grid size
+  double coef;  // (alpha * (N-1)) * (N-1), evaluated on the host in that order
+
+  template <bool kExact>
+  __device__ __forceinline__ double2 eval(const double2 *__restrict__ w, int p) const {
+    using M = Arith<kExact>;
+    const int k = p / N;
+    const int j = p - k * N;
+    const double2 c = w[p];
+    const double2 up = w[k == 0 ? p + N : p - N];
+    const double2 dn = w[k == N - 1 ? p - N : p + N];
+    double lu = M::add(up.x, dn.x);
+    double lv = M::add(up.y, dn.y);
+    if (j == 0) {
+      const double2 e = w[p + 1];
+      lu = fma(2.0, e.x, lu);
+      lv = fma(2.0, e.y, lv);
+    } else if (j == N - 1) {
+      const double2 ww = w[p - 1];
+      lu = fma(2.0, ww.x, lu);
+      lv = fma(2.0, ww.y, lv);
+    } else {
+      const double2 ww = w[p - 1];
+      const double2 e = w[p + 1];
+      lu = M::add(M::add(lu, ww.x), e.x);
+      lv = M::add(M::add(lv, ww.y), e.y);
+    }
+    lu = fma(-4.0, c.x, lu);
+    lv = fma(-4.0, c.y, lv);
+    const double u2v = M::mul(M::mul(c.x, c.x), c.y);  // shared by U and V
+    const double ru = M::sub(M::add(1.0, u2v), M::mul(4.4, c.x));
+    const double rv = M::msub(3.4, c.x, u2v);
+    return make_double2(M::mac(ru, coef, lu), M::mac(rv, coef, lv));
+  }
+};
+
+// LV pairs (src/problems/lv.c:66-87):
+//   prey  f0 = c0*y0 - d0*y0*y1,  predator f1 = d1*y0*y1 - c1*y1
+struct LvPairs {
+  template <bool kExact>
+  __device__ __forceinline__ double2 eval(const double2 *__restrict__ w, int p) const {
+    using M = Arith<kExact>;
+    const double2 c = w[p];
+    const double f0 = M::sub(M::mul(0.1, c.x), M::mul(M::mul(0.2, c.x), c.y));
+    const double f1 = M::msub(M::mul(0.4, c.x), c.y, M::mul(0.2, c.y));
+    return make_double2(f0, f1);
+  }
+};
+
+// Banded LV chain (no reference module): f_i = y_i (r_i + sum_{d=-2..2} a_{i,d} y_{i+d}),
+// terms added in order of d, band truncated at the ends of [0, n).
+struct LvBanded {
+  int n;
+  const double *__restrict__ r;  // r[n_pad]
+  const double *__restrict__ a;  // a[n_pad][5]
+
+  template <bool kExact>
+  __device__ __forceinline__ double comp(const double *__restrict__ y, int i) const {
+    using M = Arith<kExact>;
+    double acc = r[i];
+#pragma unroll
+    for (int d = -2; d <= 2; ++d) {
+      const int jj = i + d;
+      if (jj >= 0 && jj < n) acc = M::mac(acc, a[5 * i + d + 2], y[jj]);
+    }
+    return M::mul(y[i], acc);
+  }
+  template <bool kExact>
+  __device__ __forceinline__ double2 eval(const double2 *__restrict__ w, int p) const {
+    const double *y = reinterpret_cast<const double *>(w);
+    const int i = 2 * p;
+    const double f0 = comp<kExact>(y, i);
+    const double f1 = (i + 1 < n) ? comp<kExact>(y, i + 1) : 0.0;
+    return make_double2(f0, f1);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Solver state shared by all CTAs of a persistent launch and kept across
+// launches.  The step-control scalars are written back by CTA 0 only.
+// ---------------------------------------------------------------------------
+struct DevState {
+  double t, h;
+  int steps_acc, steps_rej;
+  int cur;            // which of the two y buffers holds the current y
+  int done;
+  unsigned long long step;          // attempted steps so far (slot parity)
+  unsigned long long err_slot[2];   // bit pattern of the step's error max (>= 0)
+  unsigned int bar_count;
+  unsigned int bar_gen;
+  int error;          // nonzero once a device wait ran out of time
+  int error_site;
+};
+
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Grid-wide barrier for a cooperative launch (all CTAs co-resident).  The
+// wait is bounded by timeout_ns: on expiry the CTA records an error in the
+// state and the barrier returns false; callers then leave the kernel.
+__device__ __forceinline__ bool grid_barrier(DevState *st, unsigned int nblocks,
+                                             unsigned long long timeout_ns, int site) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int *gen = &st->bar_gen;
+    const unsigned int g = *gen;
+    __threadfence();
+    const unsigned int arrived = atomicAdd(&st->bar_count, 1u);
+    int ok = 1;
+    if (arrived == nblocks - 1) {
+      st->bar_count = 0;
+      __threadfence();
+      atomicAdd(&st->bar_gen, 1u);
+    } else {
+      const unsigned long long t0 = globaltimer_ns();
+      unsigned int ns = 32;
+      while (*gen == g) {
+        if (*(volatile int *)&st->error) { ok = 0; break; }
+        if (globaltimer_ns() - t0 > timeout_ns) {
+          if (atomicCAS(&st->error, 0, 1) == 0) st->error_site = site;
+          ok = 0;
+          break;
+        }
+        __nanosleep(ns);
+        if (ns < 256) ns <<= 1;
+      }
+    }
+    __threadfence();
+    s_ok = ok && (*(volatile int *)&st->error == 0);
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// Step-size factor of include/tools.h:221-233 (AMAX 2, AMIN 0.5, ASAF 0.9).
+__device__ __forceinline__ double h_new(double h, double err, double tol, int ord) {
+  if (tol <= 0.0) return h;
+  return h * fmin(2.0, fmax(0.5, 0.9 * pow(tol / err, 1.0 / (ord + 1.0))));
+}
+
+}  // namespace rkcu

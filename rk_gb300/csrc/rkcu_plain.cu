@@ -1,0 +1,276 @@
+// Plain form of the step loop: one persistent cooperative kernel executes
+// whole embedded-RK steps with the stage order of the reference's D variant
+// (src/impl/seq/D.c:58-78 with the scatter kernels of
+// include/block-inline.h:253-320), the error max of include/tools.h:280-288
+// and the step control of include/tools.h:191-278 -- all on the device.
+//
+// Layout in HBM (component pairs as double2, every vector padded to even n):
+//   y[2]            current state and the candidate of the running step; an
+//                   accepted step flips the index, a rejected one keeps it, so
+//                   the reference's y_old restore copy (tools.h:273) is not needed
+//   w[1..s-1]       stage arguments, accumulated in scatter order
+//   dy, err         the b- and (b - b_hat)-weighted sums
+// Each stage is one grid-stride sweep over the pairs followed by a bounded grid
+// barrier (the stencil of the next stage reads neighbours written by other
+// CTAs).  The error max is reduced by warp shuffles, shared memory and one
+// 64-bit atomicMax per CTA on the bit pattern (the values are >= 0).
+#include "rkcu_plain.cuh"
+#include "rkcu.h"
+
+namespace rkcu {
+
+constexpr int kThreads = 256;
+
+template <class Prob>
+__device__ __forceinline__ const Prob &problem_of(const PlainParams &P);
+template <>
+__device__ __forceinline__ const Bruss &problem_of<Bruss>(const PlainParams &P) { return P.bruss; }
+template <>
+__device__ __forceinline__ const LvPairs &problem_of<LvPairs>(const PlainParams &P) { return P.lvp; }
+template <>
+__device__ __forceinline__ const LvBanded &problem_of<LvBanded>(const PlainParams &P) { return P.lvb; }
+
+// |e| / max(|y_new|, |y_old|), with the reference's 1.7E308 for a zero divisor
+__device__ __forceinline__ double err_ratio(double e, double yn, double yo) {
+  const double div = fmax(fabs(yn), fabs(yo));
+  return div == 0.0 ? 1.7E308 : fabs(e) / div;
+}
+
+template <class Prob, bool kExact>
+__global__ void __launch_bounds__(kThreads) plain_kernel(const __grid_constant__ PlainParams P) {
+  using M = Arith<kExact>;
+  __shared__ double hA[kMaxStages * kMaxStages];
+  __shared__ double hb[kMaxStages], hbh[kMaxStages];
+  __shared__ double s_t, s_h;
+  __shared__ int s_acc, s_rej, s_cur, s_done;
+  __shared__ unsigned long long s_step;
+  __shared__ double s_wmax[kThreads / 32];
+
+  const Prob &prob = problem_of<Prob>(P);
+  DevState *st = P.st;
+  const int s = P.s;
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gstride = gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+
+  if (threadIdx.x == 0) {
+    s_t = st->t;
+    s_h = st->h;
+    s_acc = st->steps_acc;
+    s_rej = st->steps_rej;
+    s_cur = st->cur;
+    s_done = st->done;
+    s_step = st->step;
+  }
+  __syncthreads();
+
+  bool ok = true;
+  for (int it = 0; it < P.budget; ++it) {
+    if (s_done) break;
+    // premult (src/methods.c:43-58): hA = h*A, hb = h*b, hbh = h*(b - b_hat)
+    const double h = s_h;
+    for (int idx = threadIdx.x; idx < kMaxStages * kMaxStages; idx += blockDim.x)
+      hA[idx] = h * P.A[idx];
+    if (threadIdx.x < kMaxStages) {
+      hb[threadIdx.x] = h * P.b[threadIdx.x];
+      hbh[threadIdx.x] = h * P.bh[threadIdx.x];
+    }
+    __syncthreads();
+    const double2 *__restrict__ ycur = P.y[s_cur];
+    double2 *__restrict__ ynew = P.y[s_cur ^ 1];
+
+    // first stage (block-inline.h:253-272)
+    for (int p = gtid; p < P.npairs; p += gstride) {
+      const double2 F = prob.template eval<kExact>(ycur, p);
+      const double2 Y = ycur[p];
+      for (int l = 1; l < s; ++l) {
+        double2 wv = Y;
+        if (P.nzA[l * kMaxStages]) {
+          const double a = hA[l * kMaxStages];
+          wv.x = M::mac(Y.x, a, F.x);
+          wv.y = M::mac(Y.y, a, F.y);
+        }
+        P.w[l][p] = wv;
+      }
+      P.dy[p] = make_double2(M::mul(hb[0], F.x), M::mul(hb[0], F.y));
+      P.err[p] = make_double2(M::mul(hbh[0], F.x), M::mul(hbh[0], F.y));
+    }
+    if (!(ok = grid_barrier(st, P.nblocks, P.timeout_ns, 1))) break;
+
+    // intermediate stages (block-inline.h:276-294)
+    for (int i = 1; i < s - 1; ++i) {
+      const double2 *__restrict__ wi = P.w[i];
+      const double bi = hb[i], bhi = hbh[i];
+      const bool nzb = P.nzb[i], nzbh = P.nzbh[i];
+      for (int p = gtid; p < P.npairs; p += gstride) {
+        const double2 F = prob.template eval<kExact>(wi, p);
+        for (int l = i + 1; l < s; ++l) {
+          if (!P.nzA[l * kMaxStages + i]) continue;
+          const double a = hA[l * kMaxStages + i];
+          double2 wv = P.w[l][p];
+          wv.x = M::mac(wv.x, a, F.x);
+          wv.y = M::mac(wv.y, a, F.y);
+          P.w[l][p] = wv;
+        }
+        if (nzb) {
+          double2 d = P.dy[p];
+          d.x = M::mac(d.x, bi, F.x);
+          d.y = M::mac(d.y, bi, F.y);
+          P.dy[p] = d;
+        }
+        if (nzbh) {
+          double2 e = P.err[p];
+          e.x = M::mac(e.x, bhi, F.x);
+          e.y = M::mac(e.y, bhi, F.y);
+          P.err[p] = e;
+        }
+      }
+      if (!(ok = grid_barrier(st, P.nblocks, P.timeout_ns, 2))) break;
+    }
+    if (!ok) break;
+
+    // last stage (block-inline.h:298-320) and error max (tools.h:280-288)
+    double emax = 0.0;
+    {
+      const int i = s - 1;
+      const double2 *__restrict__ wl = P.w[i];
+      const double bi = hb[i], bhi = hbh[i];
+      const bool nzb = P.nzb[i], nzbh = P.nzbh[i];
+      for (int p = gtid; p < P.npairs; p += gstride) {
+        const double2 F = prob.template eval<kExact>(wl, p);
+        double2 d = P.dy[p];
+        double2 e = P.err[p];
+        if (nzb) {
+          d.x = M::mac(d.x, bi, F.x);
+          d.y = M::mac(d.y, bi, F.y);
+        }
+        if (nzbh) {
+          e.x = M::mac(e.x, bhi, F.x);
+          e.y = M::mac(e.y, bhi, F.y);
+        }
+        const double2 Y = ycur[p];
+        const double2 yn = make_double2(M::add(Y.x, d.x), M::add(Y.y, d.y));
+        ynew[p] = yn;
+        emax = fmax(emax, err_ratio(e.x, yn.x, Y.x));
+        if (2 * p + 1 < P.n) emax = fmax(emax, err_ratio(e.y, yn.y, Y.y));
+      }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) emax = fmax(emax, __shfl_xor_sync(0xffffffffu, emax, off));
+    if (lane == 0) s_wmax[warp] = emax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double m = s_wmax[0];
+      for (int k = 1; k < kThreads / 32; ++k) m = fmax(m, s_wmax[k]);
+      atomicMax(&st->err_slot[s_step & 1], (unsigned long long)__double_as_longlong(m));
+    }
+    if (!(ok = grid_barrier(st, P.nblocks, P.timeout_ns, 3))) break;
+
+    // step control (tools.h:191-198, 235-278), taken identically by every CTA
+    if (threadIdx.x == 0) {
+      if (blockIdx.x == 0) st->err_slot[(s_step + 1) & 1] = 0ull;
+      const double errmax =
+          __longlong_as_double((long long)*(volatile unsigned long long *)&st->err_slot[s_step & 1]);
+      double t = s_t, hh = s_h;
+      int acc = s_acc, rej = s_rej, cur = s_cur;
+      if (P.tol <= 0.0) {
+        t += hh;
+        ++acc;
+        cur ^= 1;
+      } else if (errmax <= P.tol) {
+        t += hh;
+        hh = h_new(hh, errmax, P.tol, P.ord);
+        ++acc;
+        cur ^= 1;
+      } else {
+        hh = h_new(hh, errmax, P.tol, P.ord);
+        ++rej;
+      }
+      hh = fmin(hh, P.te - t);
+      s_t = t;
+      s_h = hh;
+      s_acc = acc;
+      s_rej = rej;
+      s_cur = cur;
+      s_step = s_step + 1;
+      s_done = !(t < P.te) || (P.step_limit > 0 && acc + rej >= P.step_limit);
+    }
+    __syncthreads();
+  }
+
+  if (ok && blockIdx.x == 0 && threadIdx.x == 0) {
+    st->t = s_t;
+    st->h = s_h;
+    st->steps_acc = s_acc;
+    st->steps_rej = s_rej;
+    st->cur = s_cur;
+    st->done = s_done;
+    st->step = s_step;
+  }
+}
+
+template <class Prob>
+__global__ void __launch_bounds__(kThreads) eval_rhs_kernel(Prob prob, int npairs,
+                                                            const double2 *__restrict__ y,
+                                                            double2 *__restrict__ f) {
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npairs; p += gridDim.x * blockDim.x)
+    f[p] = prob.template eval<true>(y, p);
+}
+
+template <class Prob, bool kExact>
+static cudaError_t launch_one(const PlainParams &p, int blocks_per_sm, int num_sms,
+                              cudaStream_t stream, int *grid_out) {
+  auto kern = plain_kernel<Prob, kExact>;
+  int occ = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kThreads, 0);
+  if (e != cudaSuccess) return e;
+  if (occ < 1) return cudaErrorInvalidConfiguration;
+  int per_sm = blocks_per_sm > 0 ? (blocks_per_sm < occ ? blocks_per_sm : occ) : occ;
+  int grid = per_sm * num_sms;
+  const int useful = (p.npairs + kThreads - 1) / kThreads;
+  if (grid > useful) grid = useful > 0 ? useful : 1;
+  PlainParams q = p;
+  q.nblocks = grid + (p.extra_arrivals > 0 ? p.extra_arrivals : 0);
+  void *args[] = {&q};
+  *grid_out = grid;
+  return cudaLaunchCooperativeKernel((const void *)kern, dim3(grid), dim3(kThreads), args, 0,
+                                     stream);
+}
+
+cudaError_t launch_plain(const PlainParams &p, bool exact, int blocks_per_sm, int num_sms,
+                         cudaStream_t stream, int *grid_out) {
+  switch (p.problem) {
+    case RKCU_PROBLEM_BRUSS2D_MIX:
+      return exact ? launch_one<Bruss, true>(p, blocks_per_sm, num_sms, stream, grid_out)
+                   : launch_one<Bruss, false>(p, blocks_per_sm, num_sms, stream, grid_out);
+    case RKCU_PROBLEM_LV_PAIRS:
+      return exact ? launch_one<LvPairs, true>(p, blocks_per_sm, num_sms, stream, grid_out)
+                   : launch_one<LvPairs, false>(p, blocks_per_sm, num_sms, stream, grid_out);
+    case RKCU_PROBLEM_LV_BANDED:
+      return exact ? launch_one<LvBanded, true>(p, blocks_per_sm, num_sms, stream, grid_out)
+                   : launch_one<LvBanded, false>(p, blocks_per_sm, num_sms, stream, grid_out);
+    default:
+      return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_eval_rhs(int problem, const Bruss &bruss, const LvBanded &lvb, int npairs,
+                            const double2 *y, double2 *f, cudaStream_t stream) {
+  const int grid = (npairs + kThreads - 1) / kThreads;
+  switch (problem) {
+    case RKCU_PROBLEM_BRUSS2D_MIX:
+      eval_rhs_kernel<Bruss><<<grid, kThreads, 0, stream>>>(bruss, npairs, y, f);
+      break;
+    case RKCU_PROBLEM_LV_PAIRS:
+      eval_rhs_kernel<LvPairs><<<grid, kThreads, 0, stream>>>(LvPairs{}, npairs, y, f);
+      break;
+    case RKCU_PROBLEM_LV_BANDED:
+      eval_rhs_kernel<LvBanded><<<grid, kThreads, 0, stream>>>(lvb, npairs, y, f);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace rkcu

@@ -1,0 +1,43 @@
+// Plain FP64 form: one persistent cooperative kernel runs whole steps of the
+// embedded RK method (stage combine, right-hand side, embedded error, error
+// norm, accept/reject) with the step control on the device.
+#pragma once
+
+#include "rkcu_device.cuh"
+
+namespace rkcu {
+
+struct PlainParams {
+  int npairs;        // number of component pairs (ceil(n/2))
+  int n;
+  int s, ord;
+  int problem;       // RKCU_PROBLEM_*
+  int step_limit;    // 0 = none
+  int budget;        // attempted steps this launch at most
+  int nblocks;
+  int extra_arrivals;  // test hook: phantom CTAs the barrier waits for
+  double te, tol;
+  unsigned long long timeout_ns;
+  double A[kMaxStages * kMaxStages];  // row-major, strictly lower
+  double b[kMaxStages];
+  double bh[kMaxStages];              // b - b_hat (src/impl/seq/D.c:40-41)
+  unsigned char nzA[kMaxStages * kMaxStages];
+  unsigned char nzb[kMaxStages], nzbh[kMaxStages];
+  double2 *y[2];                      // current / candidate state (ping-pong)
+  double2 *w[kMaxStages];             // w[1..s-1]
+  double2 *dy, *err;
+  DevState *st;
+  Bruss bruss;
+  LvPairs lvp;
+  LvBanded lvb;
+};
+
+// Launches one persistent kernel (cooperative) for up to p.budget steps.
+cudaError_t launch_plain(const PlainParams &p, bool exact, int blocks_per_sm, int num_sms,
+                         cudaStream_t stream, int *grid_out);
+
+// Device RHS over all pairs of y (exact arithmetic), for ode_eval_rng.
+cudaError_t launch_eval_rhs(int problem, const Bruss &bruss, const LvBanded &lvb, int npairs,
+                            const double2 *y, double2 *f, cudaStream_t stream);
+
+}  // namespace rkcu

@@ -1,0 +1,80 @@
+"""The C ABI library: loads without a GPU, exports every symbol include/rkcu.h
+declares, and its host-side logic (tableaux, argument checks) is right."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import REPO
+
+HEADER = os.path.join(REPO, "include", "rkcu.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(rkcu_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_and_python_exports_agree():
+    import rk_gb300
+    assert sorted(rk_gb300.EXPORTS) == declared_symbols()
+
+
+def test_library_exports_every_declared_symbol(rkcu_lib):
+    missing = [s for s in declared_symbols() if not hasattr(rkcu_lib, s)]
+    assert not missing, missing
+
+
+@pytest.mark.parametrize("name", ["HEUN2", "RK4", "SSPRK3", "RKF23", "DOPRI54", "VERNER65", "DOPRI87"])
+def test_builtin_tableaux_equal_oracle(name, rkcu_lib, oracle):
+    import rk_gb300
+    got = rk_gb300.builtin_method(name)
+    ref = oracle.tableau(name)
+    assert (got["s"], got["ord"], got["embedded"]) == (ref["s"], ref["ord"], ref["embedded"])
+    for k in ("A", "b", "b_hat", "c"):
+        np.testing.assert_array_equal(got[k], ref[k], err_msg=k)
+
+
+def test_unknown_method_is_rejected(rkcu_lib):
+    import rk_gb300
+    with pytest.raises(rk_gb300.RkcuError) as ei:
+        rk_gb300.builtin_method("DOPRI99")
+    assert ei.value.status == rk_gb300.ERR_INVALID
+
+
+def test_strerror_and_acc_dist(rkcu_lib):
+    import rk_gb300
+    assert rkcu_lib.rkcu_strerror(rk_gb300.ERR_TIMEOUT) == b"device wait timed out"
+    assert rk_gb300.ode_acc_dist(rk_gb300.bruss2d_mix(250)) == 500   # bruss2d-mix.c:718-721
+    assert rk_gb300.ode_acc_dist(rk_gb300.lv_pairs(10)) == 1         # lv.c:127-130
+
+
+def test_ode_start_matches_oracle(rkcu_lib, oracle):
+    import rk_gb300
+    for N in (2, 3, 17, 250):
+        np.testing.assert_array_equal(rk_gb300.ode_start(rk_gb300.bruss2d_mix(N)), oracle.bruss_start(N))
+    np.testing.assert_array_equal(rk_gb300.ode_start(rk_gb300.lv_pairs(7)), oracle.lv_pairs_start(14))
+
+
+def test_create_validates_before_touching_a_device(rkcu_lib):
+    import rk_gb300
+    h = ctypes.c_void_p()
+    bad = rk_gb300.Problem(rk_gb300.PROBLEM_BRUSS2D_MIX, 10, 3, 2e-3, None, None)  # n != 2N^2
+    assert rkcu_lib.rkcu_create(ctypes.byref(h), ctypes.byref(bad), None) == rk_gb300.ERR_INVALID
+    bad = rk_gb300.Problem(rk_gb300.PROBLEM_LV_BANDED, 10, 0, 0.0, None, None)      # no parameters
+    assert rkcu_lib.rkcu_create(ctypes.byref(h), ctypes.byref(bad), None) == rk_gb300.ERR_INVALID
+    assert rkcu_lib.rkcu_create(None, None, None) == rk_gb300.ERR_INVALID
+
+
+def test_no_cpu_fallback_without_gpu(rkcu_lib):
+    """Without a GPU the library refuses to run: it never falls back to the CPU."""
+    from conftest import have_gpu
+    if have_gpu():
+        pytest.skip("a GPU is present")
+    import rk_gb300
+    with pytest.raises(rk_gb300.RkcuError) as ei:
+        rk_gb300.Solver(rk_gb300.bruss2d_mix(8))
+    assert ei.value.status in (rk_gb300.ERR_NO_DEVICE, rk_gb300.ERR_CUDA)
