@@ -212,8 +212,7 @@ def run_ours(args):
                        stream=stream.cuda_stream)
     # ---- device-resident timing -------------------------------------------
     solver.begin(T0, TE, None, TOL, y0_device_ptr=y0_dev.data_ptr())
-    solver.advance(args.warmup)
-    solver.query()
+    st0 = solver.run(args.warmup)
     launches0 = solver.launches
     clocks = ClockSampler(local)
     if dist:
@@ -222,16 +221,16 @@ def run_ours(args):
     clocks.start()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
-    solver.advance(args.steps)
+    st = solver.run(args.steps)
     ev1.record(stream)
     ev1.synchronize()
     clk = clocks.stop()
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    st = solver.query()
     launches = solver.launches - launches0
-    steps_done = st["steps_acc"] + st["steps_rej"] - args.warmup
+    steps_done = st["steps_acc"] + st["steps_rej"] - (st0["steps_acc"] + st0["steps_rej"])
+    host_pow_steps = st["host_pow_steps"] - st0["host_pow_steps"]
     ms = ev0.elapsed_time(ev1)
     ms_max = _max_over_ranks(ms, dist, dev)
     value = ws * steps_done / (ms_max * 1e-3)
@@ -246,7 +245,7 @@ def run_ours(args):
     t = time.perf_counter()
     rc = lib.rkcu_begin(solver._h, T0, TE, ctypes.c_void_p(pinned_in.data_ptr()), 0, TOL)
     assert rc == 0, rc
-    solver.advance(args.steps)
+    solver.run(args.steps)
     rc = lib.rkcu_get_y(solver._h, ctypes.c_void_p(pinned_out.data_ptr()), 0)
     assert rc == 0, rc
     e2e_s = time.perf_counter() - t
@@ -288,6 +287,7 @@ def run_ours(args):
                 "d2h_bytes_per_step": 8.0 * n / max(1, e2e_steps),
                 "note": f"one C-ABI begin/advance/get_y of {e2e_steps} steps, pinned host y0 and y"},
         "gpu_launches": launches,
+        "host_pow_steps": host_pow_steps,
         "clocks": clk,
         "device_bytes": dev_bytes,
     }

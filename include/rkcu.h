@@ -37,10 +37,13 @@ extern "C" {
 #define RKCU_PROBLEM_LV_BANDED    2   /* banded Lotka-Volterra chain (no reference module) */
 
 /* ---- arithmetic -------------------------------------------------------- */
-#define RKCU_FP64_EXACT  0   /* reference evaluation order, no contraction: bit-identical
-                                to the reference except where CUDA pow() and glibc pow()
-                                differ in the last bit of the step-size factor */
-#define RKCU_FP64_FMA    1   /* FP64 with fused multiply-adds (fewer FP64 instructions) */
+#define RKCU_FP64_EXACT  0   /* reference evaluation order, no contraction, and the C
+                                library's pow for step sizes: bit-identical to the
+                                reference compiled without FMA contraction on the same
+                                platform (same step counts, same h, same y) */
+#define RKCU_FP64_FMA    1   /* FP64 with fused multiply-adds (fewer FP64 instructions);
+                                differs from the reference in the last bits, which can
+                                change accept/reject decisions of stiff problems */
 #define RKCU_MIXED       2   /* FP32 stage vectors, FP64 state, update and error norm */
 
 /* ---- solver variants (src/impl/seq/D.c, src/impl/seq/PipeDls.c) ------- */
@@ -80,6 +83,7 @@ typedef struct
   double h;
   int done;             /* t >= te, or the step limit was reached */
   int step_limit_reached;
+  long long host_pow_steps; /* step-size updates finished on the host (rkcu_step_size) */
 } rkcu_stats;
 
 void rkcu_options_default(rkcu_options *opt);
@@ -112,8 +116,9 @@ int rkcu_solve(rkcu_solver *s, double t0, double te, const double *y0, double *y
    begin  -- set t=t0, h=initial_stepsize (src/tools.c:25-36), y=y0 (y0 is a host
              pointer if y0_on_device == 0, else a device pointer)
    advance-- enqueue up to max_steps attempted steps on the solver's stream (async);
-             the device stops by itself at te or at the step limit
-   query  -- wait for the stream, read the counters
+             the device stops by itself at te, at the step limit, or after a step
+             whose size update is left to the host (see rkcu_step_size)
+   query  -- wait for the stream, finish such an update, read the counters
    get_y  -- copy the current y out (host or device destination) */
 int rkcu_begin(rkcu_solver *s, double t0, double te, const double *y0, int y0_on_device,
                double tol);
@@ -137,6 +142,22 @@ int rkcu_ode_start(const rkcu_problem *prob, double t, double *y0);
 int rkcu_ode_eval_rng(const rkcu_problem *prob, int i, int j, double t, const double *y,
                       double *f);
 int rkcu_ode_acc_dist(const rkcu_problem *prob);
+
+/* Step-size update of include/tools.h:221-233, h * min(2, max(0.5,
+   0.9 (tol/err)^(1/(ord+1)))), as the device controller computes it: with a
+   correctly rounded pow.  *host_pow (may be NULL) is set to 1 when the power
+   lies within 0.03 ulp of a rounding boundary -- there the C library's pow,
+   which the reference uses and which may be off by up to 0.52 ulp, can round
+   the other way, so the solver finishes such an update on the host with that
+   pow.  rkcu_step_size evaluates on the host, rkcu_step_sizes_device evaluates
+   count updates on the GPU (host arrays in and out). */
+double rkcu_step_size(double h, double err, double tol, int ord, int *host_pow);
+int rkcu_step_sizes_device(const double *h, const double *err, int count, double tol, int ord,
+                           double *out, int *host_pow);
+
+/* Run up to max_steps attempted steps and wait for them (advance + query until
+   that many steps are done or the solve is done).  stats may be NULL. */
+int rkcu_run(rkcu_solver *s, int max_steps, rkcu_stats *stats);
 
 /* Test hook: make every later launch of this solver wait at its first grid
    barrier for `extra_arrivals` CTAs that do not exist, so the bounded device

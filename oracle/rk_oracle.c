@@ -326,6 +326,11 @@ static double h_new(double h, double err, double tol, int ord)
   return h * fmin(2.0, fmax(0.5, 0.9 * pow(tol / err, 1.0 / (ord + 1.0))));
 }
 
+double ork_h_new(double h, double err, double tol, int ord)
+{
+  return h_new(h, err, tol, ord);
+}
+
 static void *solve_thread(void *argp)
 {
   thread_arg *ta = (thread_arg *) argp;

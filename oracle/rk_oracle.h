@@ -58,6 +58,9 @@ void ork_lv_pairs_start(int n, double *y0);
 double ork_eval_comp(const ork_problem *p, int i, const double *y);
 void ork_eval_all(const ork_problem *p, const double *y, double *f);
 
+/* Step-size update of include/tools.h:221-233 with the C library's pow. */
+double ork_h_new(double h, double err, double tol, int ord);
+
 /*
  * Integrate from t0 to te (the reference's solver() contract).
  * step_limit <= 0 means no limit (the reference's STEP_LIMIT=0).

@@ -49,6 +49,8 @@ def load():
         _lib = ctypes.CDLL(LIB)
         _lib.ork_solve.restype = ctypes.c_int
         _lib.ork_eval_comp.restype = ctypes.c_double
+        _lib.ork_h_new.restype = ctypes.c_double
+        _lib.ork_h_new.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_int]
     return _lib
 
 
@@ -71,6 +73,10 @@ def _problem(kind, n, grid_n=0, alpha=0.0, lv_r=None, lv_a=None):
         keep += [lr, la]
         r, a = lr.ctypes.data, la.ctypes.data
     return Problem(kind, n, grid_n, alpha, r, a), keep
+
+
+def h_new(h, err, tol, ord):
+    return load().ork_h_new(h, err, tol, ord)
 
 
 def bruss_start(N):

@@ -50,6 +50,7 @@ EXPORTS = (
     "rkcu_advance", "rkcu_query", "rkcu_get_y", "rkcu_stream", "rkcu_launch_count",
     "rkcu_device_bytes", "rkcu_ode_start", "rkcu_ode_eval_rng", "rkcu_ode_acc_dist",
     "rkcu_strerror", "rkcu_last_cuda_error", "rkcu_debug_inject_wait_timeout",
+    "rkcu_step_size", "rkcu_step_sizes_device", "rkcu_run",
 )
 
 
@@ -78,7 +79,8 @@ class Options(ctypes.Structure):
 
 class Stats(ctypes.Structure):
     _fields_ = [("steps_acc", ctypes.c_int), ("steps_rej", ctypes.c_int), ("t", ctypes.c_double),
-                ("h", ctypes.c_double), ("done", ctypes.c_int), ("step_limit_reached", ctypes.c_int)]
+                ("h", ctypes.c_double), ("done", ctypes.c_int), ("step_limit_reached", ctypes.c_int),
+                ("host_pow_steps", ctypes.c_longlong)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -120,6 +122,10 @@ def load():
     lib.rkcu_ode_eval_rng.argtypes = [P(Problem), I, I, D, V, V]
     lib.rkcu_ode_acc_dist.argtypes = [P(Problem)]
     lib.rkcu_debug_inject_wait_timeout.argtypes = [V, I]
+    lib.rkcu_step_size.restype = D
+    lib.rkcu_step_size.argtypes = [D, D, D, I, P(I)]
+    lib.rkcu_step_sizes_device.argtypes = [V, V, I, D, I, V, V]
+    lib.rkcu_run.argtypes = [V, I, P(Stats)]
     _lib = lib
     return lib
 
@@ -224,6 +230,27 @@ def ode_acc_dist(problem):
     return load().rkcu_ode_acc_dist(ctypes.byref(ps))
 
 
+def step_sizes(h, err, tol, ord, device=False):
+    """Step-size updates h * min(2, max(0.5, 0.9 (tol/err)^(1/(ord+1)))) for arrays
+    h, err as the device controller computes them (correctly rounded pow), on the
+    host or on the GPU.  Returns (values, host_pow flags)."""
+    lib = load()
+    h = np.ascontiguousarray(np.broadcast_to(h, np.shape(err)), dtype=np.float64)
+    err = np.ascontiguousarray(err, dtype=np.float64)
+    flags = np.zeros(err.size, dtype=np.int32)
+    if device:
+        out = np.empty_like(err)
+        _check(lib.rkcu_step_sizes_device(_ptr(h), _ptr(err), err.size, tol, ord, _ptr(out),
+                                          _ptr(flags)), "step_sizes_device")
+        return out, flags.astype(bool)
+    out = np.empty(err.size)
+    f = ctypes.c_int()
+    for k, (a, b) in enumerate(zip(h.ravel(), err.ravel())):
+        out[k] = lib.rkcu_step_size(a, b, tol, ord, ctypes.byref(f))
+        flags[k] = f.value
+    return out, flags.astype(bool)
+
+
 _PREC = {"exact": FP64_EXACT, "fp64": FP64_EXACT, "fma": FP64_FMA, "mixed": MIXED}
 
 
@@ -285,6 +312,12 @@ class Solver:
 
     def advance(self, max_steps):
         _check(self._lib.rkcu_advance(self._h, int(max_steps)), "rkcu_advance")
+
+    def run(self, max_steps):
+        """Run up to max_steps attempted steps and wait (rkcu_run)."""
+        st = Stats()
+        _check(self._lib.rkcu_run(self._h, int(max_steps), ctypes.byref(st)), "rkcu_run")
+        return st.as_dict()
 
     def query(self):
         st = Stats()

@@ -43,7 +43,7 @@ def _run(cmd):
 def build_cuda(verbose=False):
     os.makedirs(LIBDIR, exist_ok=True)
     os.makedirs(OBJDIR, exist_ok=True)
-    flags = [GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2",
+    flags = [GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off",
              "-I" + INCLUDE, "-I" + CSRC, "--expt-relaxed-constexpr"]
     if verbose:
         flags.append("-Xptxas=-v")

@@ -325,7 +325,21 @@ int rkcu_query(rkcu_solver *s, rkcu_stats *stats) {
   RKCU_CK(cudaSetDevice(s->opt.device));
   RKCU_CK(cudaMemcpyAsync(s->st_host, s->st, sizeof(DevState), cudaMemcpyDeviceToHost, s->stream));
   RKCU_CK(cudaStreamSynchronize(s->stream));
-  const DevState *h = s->st_host;
+  DevState *h = s->st_host;
+  if (!h->error && h->pending) {
+    // Finish the step-size update with the C library's pow, exactly as
+    // include/tools.h:221-233 writes it, then the loop increment of
+    // tools.h:196-197 and the loop test.
+    const double f = h->pend_h * std::fmin(2.0, std::fmax(0.5, 0.9 * std::pow(s->tol / h->pend_err,
+                                                                            1.0 / (s->ord + 1.0))));
+    h->h = std::fmin(f, s->te - h->t);
+    h->done = !(h->t < s->te) ||
+              (s->opt.step_limit > 0 && h->steps_acc + h->steps_rej >= s->opt.step_limit);
+    h->pending = 0;
+    ++h->host_pow_steps;
+    RKCU_CK(cudaMemcpyAsync(s->st, h, sizeof(DevState), cudaMemcpyHostToDevice, s->stream));
+    RKCU_CK(cudaStreamSynchronize(s->stream));
+  }
   if (stats) {
     stats->steps_acc = h->steps_acc;
     stats->steps_rej = h->steps_rej;
@@ -334,6 +348,7 @@ int rkcu_query(rkcu_solver *s, rkcu_stats *stats) {
     stats->done = h->done;
     stats->step_limit_reached =
         s->opt.step_limit > 0 && h->steps_acc + h->steps_rej >= s->opt.step_limit;
+    stats->host_pow_steps = h->host_pow_steps;
   }
   if (h->error) {
     std::snprintf(g_cuda_err, sizeof(g_cuda_err), "device wait timed out at site %d",
@@ -363,14 +378,60 @@ int rkcu_solve(rkcu_solver *s, double t0, double te, const double *y0, double *y
   int rc = rkcu_begin(s, t0, te, y0, 0, tol);
   if (rc != RKCU_OK) return rc;
   rkcu_stats st{};
-  for (;;) {
-    if ((rc = rkcu_advance(s, 1 << 16)) != RKCU_OK) return rc;
+  if ((rc = rkcu_query(s, &st)) != RKCU_OK) return rc;
+  while (!st.done) {
+    if ((rc = rkcu_advance(s, 1 << 20)) != RKCU_OK) return rc;
     if ((rc = rkcu_query(s, &st)) != RKCU_OK) return rc;
-    if (st.done) break;
   }
   if ((rc = rkcu_get_y(s, y, 0)) != RKCU_OK) return rc;
   if (stats) *stats = st;
   return RKCU_OK;
+}
+
+int rkcu_run(rkcu_solver *s, int max_steps, rkcu_stats *stats) {
+  if (!s) return RKCU_ERR_INVALID;
+  if (!s->begun) return RKCU_ERR_STATE;
+  rkcu_stats st{};
+  int rc = rkcu_query(s, &st);
+  if (rc != RKCU_OK) return rc;
+  const long long target = (long long)st.steps_acc + st.steps_rej + (max_steps > 0 ? max_steps : 0);
+  while (!st.done && (long long)st.steps_acc + st.steps_rej < target) {
+    const long long left = target - st.steps_acc - st.steps_rej;
+    if ((rc = rkcu_advance(s, (int)(left < (1 << 30) ? left : (1 << 30)))) != RKCU_OK) return rc;
+    if ((rc = rkcu_query(s, &st)) != RKCU_OK) return rc;
+  }
+  if (stats) *stats = st;
+  return RKCU_OK;
+}
+
+double rkcu_step_size(double h, double err, double tol, int ord, int *host_pow) {
+  bool hp = false;
+  const double r = rkcu::step_factor_h(h, err, tol, ord, &hp);
+  if (host_pow) *host_pow = hp ? 1 : 0;
+  return r;
+}
+
+int rkcu_step_sizes_device(const double *h, const double *err, int count, double tol, int ord,
+                           double *out, int *host_pow) {
+  if (!h || !err || !out || count < 0) return RKCU_ERR_INVALID;
+  if (count == 0) return RKCU_OK;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return RKCU_ERR_NO_DEVICE;
+  double *d = nullptr;
+  const size_t bytes = (size_t)count * sizeof(double);
+  double *flags = static_cast<double *>(std::malloc(bytes));
+  if (!flags) return RKCU_ERR_NOMEM;
+  cudaError_t e = cudaMalloc(&d, 4 * bytes);  // h, err, out, flags
+  if (e == cudaSuccess) e = cudaMemcpy(d, h, bytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d + count, err, bytes, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = rkcu::launch_step_sizes(d, d + count, count, tol, ord, d + 2 * count, 0);
+  if (e == cudaSuccess) e = cudaMemcpy(out, d + 2 * count, bytes, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(flags, d + 3 * count, bytes, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && host_pow)
+    for (int i = 0; i < count; ++i) host_pow[i] = flags[i] != 0.0;
+  cudaFree(d);
+  std::free(flags);
+  return e == cudaSuccess ? RKCU_OK : cuda_fail(e, "rkcu_step_sizes_device");
 }
 
 int rkcu_debug_inject_wait_timeout(rkcu_solver *s, int extra_arrivals) {

@@ -5,6 +5,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "rkcu_pow.cuh"
+
 namespace rkcu {
 
 constexpr int kMaxStages = 13;   // DOPRI87 (src/methods.c:476) is the largest tableau
@@ -153,6 +155,12 @@ struct DevState {
   unsigned int bar_gen;
   int error;          // nonzero once a device wait ran out of time
   int error_site;
+  // A step whose size update is left to the host (the accept/reject decision,
+  // t, the counters and y are already applied on the device):
+  int pending;        // 1 while the host has not finished the update
+  double pend_err;    // the step's error max
+  double pend_h;      // the step's h
+  long long host_pow_steps;  // how many updates the host finished so far
 };
 
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
@@ -199,10 +207,11 @@ __device__ __forceinline__ bool grid_barrier(DevState *st, unsigned int nblocks,
   return s_ok != 0;
 }
 
-// Step-size factor of include/tools.h:221-233 (AMAX 2, AMIN 0.5, ASAF 0.9).
-__device__ __forceinline__ double h_new(double h, double err, double tol, int ord) {
-  if (tol <= 0.0) return h;
-  return h * fmin(2.0, fmax(0.5, 0.9 * pow(tol / err, 1.0 / (ord + 1.0))));
+// Step-size update of include/tools.h:221-233 (AMAX 2, AMIN 0.5, ASAF 0.9),
+// with a correctly rounded pow; *host_pow flags the rare updates the host
+// finishes with the C library's pow (see step_factor_h).
+__device__ __forceinline__ double h_new(double h, double err, double tol, int ord, bool *host_pow) {
+  return step_factor_h(h, err, tol, ord, host_pow);
 }
 
 }  // namespace rkcu

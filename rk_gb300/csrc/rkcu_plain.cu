@@ -42,8 +42,9 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(const __grid_constant__
   __shared__ double hA[kMaxStages * kMaxStages];
   __shared__ double hb[kMaxStages], hbh[kMaxStages];
   __shared__ double s_t, s_h;
-  __shared__ int s_acc, s_rej, s_cur, s_done;
+  __shared__ int s_acc, s_rej, s_cur, s_done, s_pending;
   __shared__ unsigned long long s_step;
+  __shared__ double s_pend_err, s_pend_h;
   __shared__ double s_wmax[kThreads / 32];
 
   const Prob &prob = problem_of<Prob>(P);
@@ -61,12 +62,15 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(const __grid_constant__
     s_cur = st->cur;
     s_done = st->done;
     s_step = st->step;
+    s_pending = st->pending;
+    s_pend_err = st->pend_err;
+    s_pend_h = st->pend_h;
   }
   __syncthreads();
 
   bool ok = true;
   for (int it = 0; it < P.budget; ++it) {
-    if (s_done) break;
+    if (s_done || s_pending) break;
     // premult (src/methods.c:43-58): hA = h*A, hb = h*b, hbh = h*(b - b_hat)
     const double h = s_h;
     for (int idx = threadIdx.x; idx < kMaxStages * kMaxStages; idx += blockDim.x)
@@ -173,29 +177,41 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(const __grid_constant__
           __longlong_as_double((long long)*(volatile unsigned long long *)&st->err_slot[s_step & 1]);
       double t = s_t, hh = s_h;
       int acc = s_acc, rej = s_rej, cur = s_cur;
+      bool host_pow = false;
       if (P.tol <= 0.0) {
         t += hh;
         ++acc;
         cur ^= 1;
-      } else if (errmax <= P.tol) {
-        t += hh;
-        hh = h_new(hh, errmax, P.tol, P.ord);
-        ++acc;
-        cur ^= 1;
       } else {
-        hh = h_new(hh, errmax, P.tol, P.ord);
-        ++rej;
+        const double hn = h_new(hh, errmax, P.tol, P.ord, &host_pow);
+        if (errmax <= P.tol) {
+          t += hh;
+          ++acc;
+          cur ^= 1;
+        } else {
+          ++rej;
+        }
+        if (host_pow) {
+          s_pend_err = errmax;
+          s_pend_h = hh;
+        } else {
+          hh = hn;
+        }
       }
-      hh = fmin(hh, P.te - t);
+      s_pending = host_pow;
+      if (!host_pow) {
+        hh = fmin(hh, P.te - t);
+        s_done = !(t < P.te) || (P.step_limit > 0 && acc + rej >= P.step_limit);
+      }
       s_t = t;
       s_h = hh;
       s_acc = acc;
       s_rej = rej;
       s_cur = cur;
       s_step = s_step + 1;
-      s_done = !(t < P.te) || (P.step_limit > 0 && acc + rej >= P.step_limit);
     }
     __syncthreads();
+    if (s_pending) break;  // the host finishes this step's size update
   }
 
   if (ok && blockIdx.x == 0 && threadIdx.x == 0) {
@@ -206,6 +222,9 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(const __grid_constant__
     st->cur = s_cur;
     st->done = s_done;
     st->step = s_step;
+    st->pending = s_pending;
+    st->pend_err = s_pend_err;
+    st->pend_h = s_pend_h;
   }
 }
 
@@ -270,6 +289,27 @@ cudaError_t launch_eval_rhs(int problem, const Bruss &bruss, const LvBanded &lvb
     default:
       return cudaErrorInvalidValue;
   }
+  return cudaGetLastError();
+}
+
+}  // namespace rkcu
+
+namespace rkcu {
+
+__global__ void step_sizes_kernel(const double *__restrict__ h, const double *__restrict__ err,
+                                  int count, double tol, int ord, double *__restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool host_pow;
+  if (i < count) {
+    out[i] = h_new(h[i], err[i], tol, ord, &host_pow);
+    out[count + i] = host_pow ? 1.0 : 0.0;
+  }
+}
+
+cudaError_t launch_step_sizes(const double *h, const double *err, int count, double tol, int ord,
+                              double *out, cudaStream_t stream) {
+  if (count <= 0) return cudaSuccess;
+  step_sizes_kernel<<<(count + 255) / 256, 256, 0, stream>>>(h, err, count, tol, ord, out);
   return cudaGetLastError();
 }
 

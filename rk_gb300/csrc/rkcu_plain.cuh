@@ -40,4 +40,8 @@ cudaError_t launch_plain(const PlainParams &p, bool exact, int blocks_per_sm, in
 cudaError_t launch_eval_rhs(int problem, const Bruss &bruss, const LvBanded &lvb, int npairs,
                             const double2 *y, double2 *f, cudaStream_t stream);
 
+// Step-size updates on the device (count values), for tests of the controller.
+cudaError_t launch_step_sizes(const double *h, const double *err, int count, double tol, int ord,
+                              double *out, cudaStream_t stream);
+
 }  // namespace rkcu

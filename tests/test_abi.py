@@ -78,3 +78,44 @@ def test_no_cpu_fallback_without_gpu(rkcu_lib):
     with pytest.raises(rk_gb300.RkcuError) as ei:
         rk_gb300.Solver(rk_gb300.bruss2d_mix(8))
     assert ei.value.status in (rk_gb300.ERR_NO_DEVICE, rk_gb300.ERR_CUDA)
+
+
+def test_step_size_update_matches_c_library(rkcu_lib, oracle):
+    """Host copy of the device step-size update (correctly rounded pow) equals the
+    reference's h_new (include/tools.h:221-233, C library pow) wherever it does not
+    ask the host to finish the update, and every disagreement is flagged."""
+    import rk_gb300
+    rng = np.random.default_rng(11)
+    flagged = differ = unflagged_differ = 0
+    for ord_ in (2, 5, 6, 8):
+        err = 10 ** rng.uniform(-9, -3, 20000)
+        vals, flags = rk_gb300.step_sizes(1e-5, err, 1e-6, ord_)
+        for v, f, e in zip(vals, flags, err):
+            ref = oracle.h_new(1e-5, e, 1e-6, ord_)
+            flagged += int(f)
+            if v != ref:
+                differ += 1
+                unflagged_differ += int(not f)
+    assert unflagged_differ == 0
+    assert flagged < 0.08 * 80000      # the host finishes a few percent of updates
+
+
+def test_correctly_rounded_pow_against_decimal(rkcu_lib):
+    """Where the C library and the device controller disagree, the controller's
+    power is the correctly rounded one (60-digit decimal arithmetic decides)."""
+    from decimal import Decimal, getcontext
+    import rk_gb300
+    getcontext().prec = 60
+    rng = np.random.default_rng(3)
+    err = 10 ** rng.uniform(-9, -3, 3000)
+    vals, _ = rk_gb300.step_sizes(1.0, err, 1e-6, 5)
+    for v, e in zip(vals, err):
+        q = 1e-6 / e
+        true_pow = (Decimal(q).ln() * Decimal(1.0 / 6.0)).exp()
+        if Decimal("0.56") < true_pow < Decimal("2.2"):
+            # with h = 1 and no clamp, v = RN(0.9 * RN(pow)): RN(pow) must be the
+            # double nearest to the true power
+            cand = [np.nextafter(float(true_pow), -np.inf), float(true_pow),
+                    np.nextafter(float(true_pow), np.inf)]
+            best = min(cand, key=lambda c: abs(Decimal(c) - true_pow))
+            assert v == 0.9 * best
