@@ -72,6 +72,8 @@ typedef struct
   int device;           /* CUDA device ordinal */
   void *stream;         /* cudaStream_t to run on; NULL = a stream owned by the solver */
   double wait_timeout_s;/* limit of every device-side wait; <= 0 selects 10 s */
+  double h_init;        /* initial step size; 0 = initial_stepsize() of src/tools.c:25-36
+                           (pass the reference's own initial_stepsize() result or H_INIT) */
 } rkcu_options;
 
 /* Progress of a solve: the counters of src/tools.c:62-79 plus the current t, h. */

@@ -74,7 +74,8 @@ class Problem(ctypes.Structure):
 class Options(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("variant", ctypes.c_int),
                 ("step_limit", ctypes.c_int), ("device", ctypes.c_int),
-                ("stream", ctypes.c_void_p), ("wait_timeout_s", ctypes.c_double)]
+                ("stream", ctypes.c_void_p), ("wait_timeout_s", ctypes.c_double),
+                ("h_init", ctypes.c_double)]
 
 
 class Stats(ctypes.Structure):

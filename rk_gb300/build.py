@@ -69,9 +69,35 @@ def build_oracle():
     return os.path.join(REPO, "oracle", "_build", "librk_oracle.so")
 
 
+# Drop-in driver binaries (bin/<family>_<problem>_<variant> naming of the
+# reference's Makefile): the drop-in D.c + the stand-in runtime, one
+# configuration each, as the reference builds one binary per configuration.
+DROPIN = {
+    "cuda_bruss2d-mix_D": ["BRUSS_GRID_SIZE=250", "BRUSS_ALPHA=2E-3", "METHOD=DOPRI54", "TOL=1E-6",
+                           "T_END=0.5", "STEP_LIMIT=0"],
+    "cuda_lv_D": ["RKCU_PROBLEM_LV", "LV_COUNT=1000", "METHOD=DOPRI54", "TOL=1E-6", "T_END=10.0",
+                  "STEP_LIMIT=0"],
+}
+
+
+def build_dropin():
+    d = os.path.join(PKG, "dropin")
+    cc = shutil.which("gcc") or "cc"
+    out = []
+    for name, defs in DROPIN.items():
+        exe = os.path.join(LIBDIR, name)
+        _run([cc, "-O2", "-std=gnu11", "-Wall", "-ffp-contract=off", "-I" + os.path.join(d, "compat"),
+              "-I" + INCLUDE, *["-D" + x for x in defs], os.path.join(d, "D.c"),
+              os.path.join(d, "compat", "runtime.c"), "-L" + LIBDIR, "-lrkcu",
+              "-Wl,-rpath,$ORIGIN", "-lm", "-o", exe])
+        out.append(exe)
+    return out
+
+
 def build_all(verbose=False):
     lib = build_cuda(verbose)
     orc = build_oracle()
+    build_dropin()
     return lib, orc
 
 

@@ -94,6 +94,7 @@ void rkcu_options_default(rkcu_options *o) {
   o->device = 0;
   o->stream = nullptr;
   o->wait_timeout_s = 10.0;
+  o->h_init = 0.0;
 }
 
 const char *rkcu_strerror(int status) {
@@ -141,6 +142,7 @@ int rkcu_create(rkcu_solver **out, const rkcu_problem *prob, const rkcu_options 
   if (o.variant != RKCU_VARIANT_D) return RKCU_ERR_INVALID;
   if (o.step_limit < 0) return RKCU_ERR_INVALID;
   if (!(o.wait_timeout_s > 0.0)) o.wait_timeout_s = 10.0;
+  if (!(o.h_init >= 0.0)) return RKCU_ERR_INVALID;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= o.device || o.device < 0)
     return RKCU_ERR_NO_DEVICE;
@@ -256,7 +258,7 @@ int rkcu_begin(rkcu_solver *s, double t0, double te, const double *y0, int y0_on
   // src/tools.c:25-36 (H_INIT unset): h = min(10 tol, H / STEP_LIMIT); STEP_LIMIT 0 gives H/0
   const double H = te - t0;
   const double lim = H / static_cast<double>(s->opt.step_limit);  // 0 gives +inf as in the reference
-  const double h0 = tol > 0.0 ? std::fmin(10.0 * tol, lim) : lim;
+  const double h0 = s->opt.h_init > 0.0 ? s->opt.h_init : tol > 0.0 ? std::fmin(10.0 * tol, lim) : lim;
   DevState *h = s->st_host;
   std::memset(h, 0, sizeof(*h));
   h->t = t0;
