@@ -30,6 +30,7 @@ extern "C" {
 #define RKCU_ERR_TIMEOUT      -4   /* a device-side wait reached its time limit */
 #define RKCU_ERR_STATE        -5   /* call out of order (e.g. advance before begin) */
 #define RKCU_ERR_NO_DEVICE    -6   /* no CUDA device, or not an sm_103 device */
+#define RKCU_ERR_TOO_LARGE    -7   /* system larger than rkcu_solve_noalloc accepts */
 
 /* ---- problems (include/ode.h modules) ---------------------------------- */
 #define RKCU_PROBLEM_BRUSS2D_MIX  0   /* src/problems/bruss2d-mix.c */
@@ -166,6 +167,28 @@ int rkcu_run(rkcu_solver *s, int max_steps, rkcu_stats *stats);
    wait runs out and the call reports RKCU_ERR_TIMEOUT.  0 switches it off.
    It lets tests exercise the timeout path without faulting or hanging a GPU. */
 int rkcu_debug_inject_wait_timeout(rkcu_solver *s, int extra_arrivals);
+
+/* Allocation-free solve.  This entry point has no counterpart in the reference;
+   it serves callers that must not allocate device memory: an application that
+   owns all device memory through its own pool or a fixed budget (a simulation
+   that reserves HBM at start-up, a plugin inside another framework's context)
+   or a latency-critical loop that cannot take cudaFree's device-wide
+   synchronisation.  It runs the same FP64 step loop as rkcu_solve for
+   BRUSS2D-MIX or LV pairs with a built-in tableau (method name), reading y0
+   from and writing y to the caller's DEVICE buffers (n doubles each), and calls
+   no cudaMalloc, cudaFree or other allocating routine: every piece of scratch
+   (state vectors, stage vectors, step-control state) lives in one 8 MiB + 256 B
+   static device array that each GPU loading the library holds until the process
+   exits.  Limit: n <= 65536 components (e.g. BRUSS2D-MIX up to N = 181);
+   larger systems return RKCU_ERR_TOO_LARGE.  The first call on a device looks up
+   the array's device address (once per device, with that device current); make
+   that first call before any stream capture.  All calls share the one array, so
+   calls whose GPU work overlaps in time (other host threads, other streams)
+   race and corrupt each other; serialise them.  stream is a cudaStream_t
+   (NULL = the default stream); stats may be NULL. */
+int rkcu_solve_noalloc(const rkcu_problem *prob, const char *method, int precision,
+                       int step_limit, double t0, double te, const double *y0_dev,
+                       double *y_dev, double tol, void *stream, rkcu_stats *stats);
 
 const char *rkcu_strerror(int status);
 const char *rkcu_last_cuda_error(void);

@@ -27,6 +27,7 @@ ERR_NOMEM = -3
 ERR_TIMEOUT = -4
 ERR_STATE = -5
 ERR_NO_DEVICE = -6
+ERR_TOO_LARGE = -7
 
 PROBLEM_BRUSS2D_MIX = 0
 PROBLEM_LV_PAIRS = 1
@@ -50,7 +51,7 @@ EXPORTS = (
     "rkcu_advance", "rkcu_query", "rkcu_get_y", "rkcu_stream", "rkcu_launch_count",
     "rkcu_device_bytes", "rkcu_ode_start", "rkcu_ode_eval_rng", "rkcu_ode_acc_dist",
     "rkcu_strerror", "rkcu_last_cuda_error", "rkcu_debug_inject_wait_timeout",
-    "rkcu_step_size", "rkcu_step_sizes_device", "rkcu_run",
+    "rkcu_step_size", "rkcu_step_sizes_device", "rkcu_run", "rkcu_solve_noalloc",
 )
 
 
@@ -127,6 +128,7 @@ def load():
     lib.rkcu_step_size.argtypes = [D, D, D, I, P(I)]
     lib.rkcu_step_sizes_device.argtypes = [V, V, I, D, I, V, V]
     lib.rkcu_run.argtypes = [V, I, P(Stats)]
+    lib.rkcu_solve_noalloc.argtypes = [P(Problem), ctypes.c_char_p, I, I, D, D, V, V, D, V, P(Stats)]
     _lib = lib
     return lib
 

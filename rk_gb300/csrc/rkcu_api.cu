@@ -106,6 +106,7 @@ const char *rkcu_strerror(int status) {
     case RKCU_ERR_TIMEOUT: return "device wait timed out";
     case RKCU_ERR_STATE: return "call out of order";
     case RKCU_ERR_NO_DEVICE: return "no usable CUDA device";
+    case RKCU_ERR_TOO_LARGE: return "system larger than the allocation-free limit (65536 components)";
     default: return "unknown status";
   }
 }
