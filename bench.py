@@ -46,7 +46,7 @@ FP64_GOPS_MEASURED = 505.0
 # FP64 instructions per component-step of the DOPRI5(4) loop on BRUSS2D-MIX
 # (counted from the kernel: 7 right-hand sides of 9.5/7.5 FP64 ops per
 # component, 31 nonzero tableau products, the update and the error norm)
-FP64_OPS_PER_COMP = {"exact": 128.0, "fma": 85.0}
+FP64_OPS_PER_COMP = {"exact": 128.0, "fma": 85.0, "mixed": 12.0}
 
 
 def _peaks():
@@ -265,13 +265,14 @@ def run_ours(args):
     per_step_bytes = 16.0 * n
     launch_s = ms * 1e-3 / max(1, launches)
     achieved = per_step_bytes * steps_done / max(1, launches) / launch_s / 1e9
-    fp64_ops = FP64_OPS_PER_COMP["exact" if args.precision == "exact" else "fma"] * n * steps_done
+    fp64_ops = FP64_OPS_PER_COMP[args.precision] * n * steps_done
     fp64_achieved = fp64_ops / (ms * 1e-3) / 1e9
     line = {
         "metric": f"BRUSS2D-MIX N={args.grid} {args.method} steps/s", "value": value, "unit": "steps/s",
         "n_gpus": ws, "steps": steps_done, "warmup": args.warmup,
         "ms_per_step": ms_max / max(1, steps_done), "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision != "mixed" else "f32 stages / f64 state",
         "data": "synthetic (ode_start initial values of BRUSS2D-MIX)",
         "config": {"workload": f"bruss2d-mix N={args.grid} n={n} {args.method} tol=1e-6 t=[0,0.5]",
                    "grid_n": args.grid, "alpha": ALPHA, "method": args.method,
@@ -282,7 +283,7 @@ def run_ours(args):
                      "kernel": "plain_kernel (persistent, all stages of K steps)"},
         "fp64_roofline": {"achieved": fp64_achieved, "peak": FP64_GOPS_MEASURED,
                           "unit": "G FP64 instr/s", "frac": fp64_achieved / FP64_GOPS_MEASURED,
-                          "ops_per_component_step": FP64_OPS_PER_COMP["exact" if args.precision == "exact" else "fma"]},
+                          "ops_per_component_step": FP64_OPS_PER_COMP[args.precision]},
         "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": 8.0 * n / max(1, e2e_steps),
                 "d2h_bytes_per_step": 8.0 * n / max(1, e2e_steps),
                 "note": f"one C-ABI begin/advance/get_y of {e2e_steps} steps, pinned host y0 and y"},
@@ -312,8 +313,9 @@ def main():
     ap.add_argument("--method", default="DOPRI54")
     ap.add_argument("--grid", type=int, default=GRID_N,
                     help="grid size N (2000 is the benchmark; smaller only for profiling)")
-    ap.add_argument("--precision", default="exact", choices=["exact", "fma"],
-                    help="exact (default): bit-identical to the reference; fma: fewer FP64 instructions")
+    ap.add_argument("--precision", default="exact", choices=["exact", "fma", "mixed"],
+                    help="exact (default): bit-identical to the reference; fma: fewer FP64 "
+                         "instructions; mixed: FP32 stage vectors (the N=4000 configuration)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

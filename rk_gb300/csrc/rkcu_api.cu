@@ -8,6 +8,7 @@
 #include <new>
 
 #include "rkcu.h"
+#include "rkcu_mixed.cuh"
 #include "rkcu_plain.cuh"
 
 using rkcu::DevState;
@@ -71,6 +72,8 @@ struct rkcu_solver {
   double2 *y[2] = {nullptr, nullptr};
   double2 *stage = nullptr;  // w[1..s-1], dy, err
   int stage_vectors = 0;
+  float2 *mstage = nullptr;  // mixed form: f0, y32, S[2..s-1], dys, dyc, err
+  int mstage_vectors = 0;
   double *lv_r = nullptr, *lv_a = nullptr;
   DevState *st = nullptr;
   DevState *st_host = nullptr;  // pinned
@@ -120,6 +123,7 @@ int rkcu_destroy(rkcu_solver *s) {
   cudaFree(s->y[0]);
   cudaFree(s->y[1]);
   cudaFree(s->stage);
+  cudaFree(s->mstage);
   cudaFree(s->lv_r);
   cudaFree(s->lv_a);
   cudaFree(s->st);
@@ -139,7 +143,9 @@ int rkcu_create(rkcu_solver **out, const rkcu_problem *prob, const rkcu_options 
     o = *opt;
   else
     rkcu_options_default(&o);
-  if (o.precision != RKCU_FP64_EXACT && o.precision != RKCU_FP64_FMA) return RKCU_ERR_INVALID;
+  if (o.precision != RKCU_FP64_EXACT && o.precision != RKCU_FP64_FMA && o.precision != RKCU_MIXED)
+    return RKCU_ERR_INVALID;
+  if (o.precision == RKCU_MIXED && prob->problem != RKCU_PROBLEM_BRUSS2D_MIX) return RKCU_ERR_INVALID;
   if (o.variant != RKCU_VARIANT_D) return RKCU_ERR_INVALID;
   if (o.step_limit < 0) return RKCU_ERR_INVALID;
   if (!(o.wait_timeout_s > 0.0)) o.wait_timeout_s = 10.0;
@@ -238,7 +244,22 @@ int rkcu_begin(rkcu_solver *s, double t0, double te, const double *y0, int y0_on
   if (!(te == te) || !(t0 == t0)) return RKCU_ERR_INVALID;
   if (tol <= 0.0 && s->opt.step_limit <= 0) return RKCU_ERR_INVALID;  // fixed step needs a limit
   RKCU_CK(cudaSetDevice(s->opt.device));
-  const int need = s->s + 1;  // w[1..s-1], dy, err
+  if (s->opt.precision == RKCU_MIXED) {
+    const int mneed = s->s + 3;  // f0, y32, S[2..s-1], dys, dyc, err
+    if (s->mstage_vectors < mneed) {
+      if (s->mstage) {
+        RKCU_CK(cudaStreamSynchronize(s->stream));
+        cudaFree(s->mstage);
+        s->dev_bytes -= (long long)s->mstage_vectors * s->npairs * sizeof(float2);
+        s->mstage = nullptr;
+        s->mstage_vectors = 0;
+      }
+      RKCU_CK(cudaMalloc(&s->mstage, (size_t)mneed * s->npairs * sizeof(float2)));
+      s->mstage_vectors = mneed;
+      s->dev_bytes += (long long)mneed * s->npairs * sizeof(float2);
+    }
+  }
+  const int need = s->opt.precision == RKCU_MIXED ? 0 : s->s + 1;  // w[1..s-1], dy, err
   if (s->stage_vectors < need) {
     if (s->stage) {
       RKCU_CK(cudaStreamSynchronize(s->stream));
@@ -279,6 +300,51 @@ int rkcu_advance(rkcu_solver *s, int max_steps) {
   if (!s->begun) return RKCU_ERR_STATE;
   if (max_steps <= 0) return RKCU_OK;
   RKCU_CK(cudaSetDevice(s->opt.device));
+  if (s->opt.precision == RKCU_MIXED) {
+    rkcu::MixedParams m;
+    std::memset(&m, 0, sizeof(m));
+    m.npairs = (int)s->npairs;
+    m.n = s->prob.n;
+    m.s = s->s;
+    m.ord = s->ord;
+    m.step_limit = s->opt.step_limit;
+    m.budget = max_steps;
+    m.te = s->te;
+    m.tol = s->tol;
+    m.timeout_ns = (unsigned long long)(s->opt.wait_timeout_s * 1e9);
+    m.extra_arrivals = s->extra_arrivals;
+    for (int i = 0; i < kMaxStages; ++i) {
+      double rs = 0.0;
+      for (int j = 0; j < kMaxStages; ++j) {
+        m.A[i * kMaxStages + j] = s->A[i * kMaxStages + j];
+        m.nzA[i * kMaxStages + j] = s->A[i * kMaxStages + j] != 0.0;
+        rs += s->A[i * kMaxStages + j];
+      }
+      m.csum[i] = rs;
+      m.b[i] = s->b[i];
+      m.bh[i] = s->bh[i];
+      m.bsum += s->b[i];
+      m.bhsum += s->bh[i];
+    }
+    m.y[0] = s->y[0];
+    m.y[1] = s->y[1];
+    const size_t np = s->npairs;
+    m.f0 = s->mstage;
+    m.y32 = s->mstage + np;
+    for (int l = 2; l < s->s; ++l) m.S[l] = s->mstage + (size_t)l * np;
+    m.dys = s->mstage + (size_t)s->s * np;
+    m.dyc = s->mstage + (size_t)(s->s + 1) * np;
+    m.err = s->mstage + (size_t)(s->s + 2) * np;
+    m.st = s->st;
+    m.bruss.N = s->prob.grid_n;
+    m.bruss.coef = bruss_coef(&s->prob);
+    int grid = 0;
+    cudaError_t e = rkcu::launch_mixed(m, s->num_sms, s->stream, &grid);
+    if (e != cudaSuccess) return cuda_fail(e, "mixed kernel launch");
+    s->last_grid = grid;
+    ++s->launches;
+    return RKCU_OK;
+  }
   rkcu::PlainParams p;
   std::memset(&p, 0, sizeof(p));
   p.npairs = (int)s->npairs;
