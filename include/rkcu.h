@@ -168,6 +168,47 @@ int rkcu_run(rkcu_solver *s, int max_steps, rkcu_stats *stats);
    It lets tests exercise the timeout path without faulting or hanging a GPU. */
 int rkcu_debug_inject_wait_timeout(rkcu_solver *s, int extra_arrivals);
 
+/* ---- batched and served solves ------------------------------------------
+   Many independent instances (each its own problem size and parameters, t,
+   h, tolerance) advanced together by one persistent kernel: a sweep is one
+   attempted step of every active instance, stages run over equal-size chunks
+   of all instances, the step control runs on the device per instance.  The
+   reference solves one instance per process (src/main.c:92); these entry
+   points batch its solver() over instances.  Device memory comes from one
+   arena sized at creation; rkcu_batch_add admits an instance only if its
+   footprint (rkcu_batch_footprint) fits, and returns RKCU_ERR_NOMEM without
+   side effects otherwise, so a serving loop can queue it and retry after
+   finished instances are taken.  Arithmetic per instance is the exact (or
+   FMA) FP64 step loop with the correctly rounded step-size pow; an instance's
+   result does not depend on which other instances share the batch. */
+typedef struct rkcu_batch rkcu_batch;
+
+long long rkcu_batch_footprint(const rkcu_problem *prob, int stages);
+int rkcu_batch_create(rkcu_batch **out, long long arena_bytes, int max_instances,
+                      const char *method, const rkcu_options *opt);
+int rkcu_batch_destroy(rkcu_batch *b);
+/* Admit an instance (host y0 of n doubles, integrate t0..te with tol); *slot
+   receives its slot.  RKCU_ERR_NOMEM: no room (arena or slots) right now. */
+int rkcu_batch_add(rkcu_batch *b, const rkcu_problem *prob, double t0, double te, double tol,
+                   const double *y0, long long host_id, int *slot);
+/* Run up to max_sweeps sweeps (one launch, replayed from a CUDA graph);
+   *active_left receives the number of instances still integrating. */
+int rkcu_batch_run(rkcu_batch *b, int max_sweeps, int *active_left);
+/* Slots that finished since the last call (up to capacity). */
+int rkcu_batch_finished(rkcu_batch *b, int *slots, int capacity, int *count);
+/* Copy a finished instance's y out (host, may be NULL), its counters and id,
+   and free its slot and arena space. */
+int rkcu_batch_take(rkcu_batch *b, int slot, double *y, rkcu_stats *stats, long long *host_id);
+/* Autotuner: time real sweeps for each block size x chunk size candidate and
+   keep the fastest per active pair-step (results are unaffected: the
+   arithmetic per component does not depend on the shape). */
+int rkcu_batch_tune(rkcu_batch *b, int sweeps_per_trial, double *best_ns_per_pair_step);
+int rkcu_batch_set_tuning(rkcu_batch *b, int threads, int chunk_pairs, int blocks_per_sm,
+                          int use_graph);
+int rkcu_batch_get_tuning(rkcu_batch *b, int *threads, int *chunk_pairs, int *blocks_per_sm);
+int rkcu_batch_info(rkcu_batch *b, int *active, long long *free_bytes, long long *launches);
+void *rkcu_batch_stream(rkcu_batch *b);
+
 /* Allocation-free solve.  This entry point has no counterpart in the reference;
    it serves callers that must not allocate device memory: an application that
    owns all device memory through its own pool or a fixed budget (a simulation

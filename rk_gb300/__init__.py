@@ -52,6 +52,9 @@ EXPORTS = (
     "rkcu_device_bytes", "rkcu_ode_start", "rkcu_ode_eval_rng", "rkcu_ode_acc_dist",
     "rkcu_strerror", "rkcu_last_cuda_error", "rkcu_debug_inject_wait_timeout",
     "rkcu_step_size", "rkcu_step_sizes_device", "rkcu_run", "rkcu_solve_noalloc",
+    "rkcu_batch_footprint", "rkcu_batch_create", "rkcu_batch_destroy", "rkcu_batch_add",
+    "rkcu_batch_run", "rkcu_batch_finished", "rkcu_batch_take", "rkcu_batch_tune",
+    "rkcu_batch_set_tuning", "rkcu_batch_get_tuning", "rkcu_batch_info", "rkcu_batch_stream",
 )
 
 
@@ -128,6 +131,21 @@ def load():
     lib.rkcu_step_size.argtypes = [D, D, D, I, P(I)]
     lib.rkcu_step_sizes_device.argtypes = [V, V, I, D, I, V, V]
     lib.rkcu_run.argtypes = [V, I, P(Stats)]
+    LL = ctypes.c_longlong
+    lib.rkcu_batch_footprint.restype = LL
+    lib.rkcu_batch_footprint.argtypes = [P(Problem), I]
+    lib.rkcu_batch_create.argtypes = [P(V), LL, I, ctypes.c_char_p, P(Options)]
+    lib.rkcu_batch_destroy.argtypes = [V]
+    lib.rkcu_batch_add.argtypes = [V, P(Problem), D, D, D, V, LL, P(I)]
+    lib.rkcu_batch_run.argtypes = [V, I, P(I)]
+    lib.rkcu_batch_finished.argtypes = [V, V, I, P(I)]
+    lib.rkcu_batch_take.argtypes = [V, I, V, P(Stats), P(LL)]
+    lib.rkcu_batch_tune.argtypes = [V, I, P(D)]
+    lib.rkcu_batch_set_tuning.argtypes = [V, I, I, I, I]
+    lib.rkcu_batch_get_tuning.argtypes = [V, P(I), P(I), P(I)]
+    lib.rkcu_batch_info.argtypes = [V, P(I), P(LL), P(LL)]
+    lib.rkcu_batch_stream.restype = V
+    lib.rkcu_batch_stream.argtypes = [V]
     lib.rkcu_solve_noalloc.argtypes = [P(Problem), ctypes.c_char_p, I, I, D, D, V, V, D, V, P(Stats)]
     _lib = lib
     return lib
@@ -355,6 +373,118 @@ class Solver:
     def close(self):
         if getattr(self, "_h", None):
             self._lib.rkcu_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def footprint(problem, stages=7):
+    """Device bytes an instance needs in a Batch arena (admission size)."""
+    ps = problem.cstruct()
+    return load().rkcu_batch_footprint(ctypes.byref(ps), stages)
+
+
+class Batch:
+    """Many independent solves advanced together on one GPU (rkcu_batch_*).
+
+    add() admits an instance if its footprint fits in the arena (else returns
+    None: admission refused, try again after take()); run() advances every
+    active instance by up to `sweeps` attempted steps; finished() lists slots
+    whose solve is done; take() returns (y, stats, host_id) and frees the slot."""
+
+    def __init__(self, arena_bytes, max_instances, method="DOPRI54", precision="exact",
+                 device=0, stream=None, step_limit=0, wait_timeout_s=10.0):
+        lib = load()
+        self._lib = lib
+        opt = Options()
+        lib.rkcu_options_default(ctypes.byref(opt))
+        opt.precision = _PREC[precision] if isinstance(precision, str) else int(precision)
+        opt.step_limit = int(step_limit)
+        opt.device = int(device)
+        opt.stream = stream
+        opt.wait_timeout_s = float(wait_timeout_s)
+        h = ctypes.c_void_p()
+        _check(lib.rkcu_batch_create(ctypes.byref(h), int(arena_bytes), int(max_instances),
+                                     method.encode(), ctypes.byref(opt)), "rkcu_batch_create")
+        self._h = h
+        self._n = {}
+
+    def add(self, problem, y0, t0, te, tol, host_id=-1):
+        y0 = np.ascontiguousarray(y0, dtype=np.float64)
+        ps = problem.cstruct()
+        slot = ctypes.c_int(-1)
+        rc = self._lib.rkcu_batch_add(self._h, ctypes.byref(ps), t0, te, tol, _ptr(y0),
+                                      int(host_id), ctypes.byref(slot))
+        if rc == ERR_NOMEM:
+            return None
+        _check(rc, "rkcu_batch_add")
+        self._n[slot.value] = problem.n
+        return slot.value
+
+    def run(self, sweeps):
+        left = ctypes.c_int()
+        _check(self._lib.rkcu_batch_run(self._h, int(sweeps), ctypes.byref(left)), "rkcu_batch_run")
+        return left.value
+
+    def finished(self):
+        out = []
+        buf = np.zeros(1024, dtype=np.int32)
+        cnt = ctypes.c_int()
+        while True:
+            _check(self._lib.rkcu_batch_finished(self._h, _ptr(buf), buf.size, ctypes.byref(cnt)),
+                   "rkcu_batch_finished")
+            out.extend(int(x) for x in buf[:cnt.value])
+            if cnt.value < buf.size:
+                return out
+
+    def take(self, slot):
+        y = np.empty(self._n[slot])
+        st = Stats()
+        hid = ctypes.c_longlong()
+        _check(self._lib.rkcu_batch_take(self._h, int(slot), _ptr(y), ctypes.byref(st),
+                                         ctypes.byref(hid)), "rkcu_batch_take")
+        del self._n[slot]
+        return y, st.as_dict(), hid.value
+
+    def tune(self, sweeps_per_trial=2):
+        best = ctypes.c_double()
+        _check(self._lib.rkcu_batch_tune(self._h, int(sweeps_per_trial), ctypes.byref(best)),
+               "rkcu_batch_tune")
+        return best.value
+
+    def set_tuning(self, threads=256, chunk_pairs=1024, blocks_per_sm=0, use_graph=True):
+        _check(self._lib.rkcu_batch_set_tuning(self._h, threads, chunk_pairs, blocks_per_sm,
+                                               int(bool(use_graph))), "rkcu_batch_set_tuning")
+
+    def tuning(self):
+        t, c, b = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _check(self._lib.rkcu_batch_get_tuning(self._h, ctypes.byref(t), ctypes.byref(c),
+                                               ctypes.byref(b)), "rkcu_batch_get_tuning")
+        return dict(threads=t.value, chunk_pairs=c.value, blocks_per_sm=b.value)
+
+    def info(self):
+        a, fb, la = ctypes.c_int(), ctypes.c_longlong(), ctypes.c_longlong()
+        _check(self._lib.rkcu_batch_info(self._h, ctypes.byref(a), ctypes.byref(fb),
+                                         ctypes.byref(la)), "rkcu_batch_info")
+        return dict(active=a.value, free_bytes=fb.value, launches=la.value)
+
+    @property
+    def stream(self):
+        return self._lib.rkcu_batch_stream(self._h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.rkcu_batch_destroy(self._h)
             self._h = None
 
     def __del__(self):
