@@ -23,6 +23,8 @@ host thread) on the same workload instead.
 """
 import argparse
 import json
+
+import numpy as np
 import os
 import statistics
 import subprocess
@@ -304,8 +306,122 @@ def run_ours(args):
     return 0
 
 
+def run_batched(args):
+    """Batched form: a seeded sample of the 4096-instance BRUSS2D-MIX distribution
+    (N log-uniform [16,512], alpha U[1e-3,1e-2], tol log-uniform [1e-8,1e-4],
+    DOPRI5(4), t in [0, 0.5]) in one batch; solves/s with y0 already in HBM, and
+    the same instances' work through the plain form and the CPU port for comparison."""
+    import concurrent.futures as cf
+
+    import torch
+
+    import rk_gb300 as rk
+    from rk_gb300 import workloads
+
+    insts = workloads.batched_instances(4096, seed=2024)
+    rng = np.random.default_rng(5)
+    sample = [insts[i] for i in sorted(rng.choice(len(insts), args.instances, replace=False))]
+    probs = [rk.bruss2d_mix(d["grid_n"], d["alpha"]) for d in sample]
+    y0s = [rk.ode_start(p) for p in probs]
+    arena = sum(rk.footprint(p, 7) for p in probs) + (64 << 20)
+    torch.cuda.init()
+    with rk.Batch(arena, len(sample) + 1, precision=args.precision) as b:
+        t_e2e = time.perf_counter()
+        for k, (p, y0, d) in enumerate(zip(probs, y0s, sample)):
+            assert b.add(p, y0, d["t0"], d["te"], d["tol"], host_id=k) is not None
+        torch.cuda.synchronize()
+        tuned_ns = b.tune(2)
+        stream = torch.cuda.ExternalStream(b.stream)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        clocks = ClockSampler(0)
+        clocks.start()
+        ev0.record(stream)
+        sweeps = 0
+        while b.run(args.sweeps_per_launch) > 0:
+            sweeps += args.sweeps_per_launch
+        ev1.record(stream)
+        ev1.synchronize()
+        clk = clocks.stop()
+        ms = ev0.elapsed_time(ev1)
+        results = {}
+        for slot in b.finished():
+            y, st, hid = b.take(slot)
+            results[hid] = (y, st)
+        e2e_s = time.perf_counter() - t_e2e
+        info = b.info()
+        tuning = b.tuning()
+    comp_steps = sum(2 * d["grid_n"] ** 2 * (results[k][1]["steps_acc"] + results[k][1]["steps_rej"])
+                     for k, d in enumerate(sample))
+    value = len(sample) / (ms * 1e-3)
+
+    # plain form on a sub-sample (one solve after another), same instance distribution
+    sub = list(range(0, len(sample), max(1, len(sample) // args.plain_sample)))[: args.plain_sample]
+    t = time.perf_counter()
+    plain_cs = 0
+    for k in sub:
+        with rk.Solver(probs[k], method="DOPRI54", precision=args.precision) as s:
+            y, st = s.solve(0.0, 0.5, y0s[k], sample[k]["tol"])
+        plain_cs += 2 * sample[k]["grid_n"] ** 2 * (st["steps_acc"] + st["steps_rej"])
+    plain_s = time.perf_counter() - t
+    sub_cs = sum(2 * sample[k]["grid_n"] ** 2 * (results[k][1]["steps_acc"] + results[k][1]["steps_rej"])
+                 for k in sub)
+    # the plain form's solves/s on the whole sample, scaled by component-steps
+    plain_value = len(sample) / (plain_s * comp_steps / max(1, sub_cs))
+
+    line = {
+        "metric": "batched BRUSS2D-MIX solves/s (4096-instance distribution)", "value": value,
+        "unit": "solves/s", "n_gpus": 1, "steps": sweeps, "warmup": 0,
+        "ms_per_step": ms / max(1, sweeps), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded instance list)",
+        "config": {"workload": f"batched: {len(sample)} of 4096 seeded instances (seed 2024)",
+                   "precision": args.precision, "tuning": tuning,
+                   "tuned_ns_per_pair_step": tuned_ns,
+                   "component_steps": comp_steps},
+        "component_steps_per_s": comp_steps / (ms * 1e-3),
+        "plain_form": {"value": plain_value, "unit": "solves/s",
+                       "sample": f"{len(sub)} instances solved one after another, scaled by work"},
+        "e2e": {"value": len(sample) / e2e_s, "unit": "solves/s",
+                "h2d_bytes_per_step": sum(8 * p.n for p in probs) / max(1, sweeps),
+                "d2h_bytes_per_step": sum(8 * p.n for p in probs) / max(1, sweeps)},
+        "gpu_launches": info["launches"], "clocks": clk,
+    }
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import rk_oracle
+        rk_oracle.load()
+        threads = os.cpu_count() or 1
+        order = sorted(range(len(sample)), key=lambda k: workloads.estimated_work(sample[k]))
+        picked, budget = [], 15.0 * threads / 1e-8  # about 15 s of CPU time at ~1e8 comp-steps/s/core
+        acc = 0.0
+        for k in order:
+            if acc + workloads.estimated_work(sample[k]) > budget:
+                continue
+            picked.append(k)
+            acc += workloads.estimated_work(sample[k])
+        def one(k):
+            d = sample[k]
+            return rk_oracle.solve(rk_oracle.BRUSS2D_MIX, y0s[k], "DOPRI54", 0.0, 0.5, d["tol"],
+                                   grid_n=d["grid_n"], alpha=d["alpha"], threads=1)
+        t = time.perf_counter()
+        with cf.ThreadPoolExecutor(threads) as ex:
+            outs = list(ex.map(one, picked))
+        cpu_s = time.perf_counter() - t
+        cpu_cs = sum(2 * sample[k]["grid_n"] ** 2 * (o[1]["steps_acc"] + o[1]["steps_rej"])
+                     for k, o in zip(picked, outs))
+        line["cpu_baseline"] = {"value": len(sample) / (cpu_s * comp_steps / max(1, cpu_cs)),
+                                "unit": "solves/s", "cores": threads, "kind": "port",
+                                "sample": f"{len(picked)} of the instances, one per thread "
+                                          f"({cpu_s:.1f} s), scaled by work"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--workload", default="plain", choices=["plain", "batched"])
+    ap.add_argument("--instances", type=int, default=1024)
+    ap.add_argument("--sweeps-per-launch", type=int, default=256)
+    ap.add_argument("--plain-sample", type=int, default=32)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
@@ -322,6 +438,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batched":
+        return run_batched(args)
     return run_ours(args)
 
 
