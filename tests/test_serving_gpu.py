@@ -14,7 +14,7 @@ def _requests(count=36, seed=4):
     rng = np.random.default_rng(seed)
     out, t = [], 0.0
     for k in range(count):
-        t += rng.exponential(0.004)
+        t += rng.exponential(0.0005)
         if k % 2 == 0:
             out.append(dict(kind="bruss", arrival=t, grid_n=int(rng.integers(8, 48)), alpha=2e-3,
                             tol=1e-6, t0=0.0, te=0.5))
@@ -27,7 +27,7 @@ def _requests(count=36, seed=4):
 def test_serving_admits_by_footprint_and_matches_solo_results():
     reqs = _requests()
     fps = [rk.footprint(make_request_problem(r)[0], 7) for r in reqs]
-    arena = int(sum(sorted(fps)[-6:]))          # room for about six of the largest at once
+    arena = int(sum(sorted(fps)[-2:]))          # room for about two of the largest at once
     loop = ServingLoop(arena, max_instances=64, sweeps_per_launch=8)
     try:
         out = loop.serve(reqs, keep_results=True)
