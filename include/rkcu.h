@@ -49,7 +49,9 @@ extern "C" {
 
 /* ---- solver variants (src/impl/seq/D.c, src/impl/seq/PipeDls.c) ------- */
 #define RKCU_VARIANT_D           0   /* stage vectors w_1..w_{s-1}, dy, err in HBM */
-#define RKCU_VARIANT_LOWSTORAGE  1   /* PipeDls idea: reduced stage storage */
+#define RKCU_VARIANT_LOWSTORAGE  1   /* PipeDls idea: wavefront over row blocks, stage
+                                        vectors in ring buffers (2n + O(s^2 B) doubles);
+                                        BRUSS2D-MIX, FP64 */
 
 typedef struct rkcu_solver rkcu_solver;
 
@@ -75,6 +77,8 @@ typedef struct
   double wait_timeout_s;/* limit of every device-side wait; <= 0 selects 10 s */
   double h_init;        /* initial step size; 0 = initial_stepsize() of src/tools.c:25-36
                            (pass the reference's own initial_stepsize() result or H_INIT) */
+  int block_rows;       /* RKCU_VARIANT_LOWSTORAGE: grid rows per pipeline block (the
+                           reference's BLOCKSIZE in rows, config.h:97-98); 0 = automatic */
 } rkcu_options;
 
 /* Progress of a solve: the counters of src/tools.c:62-79 plus the current t, h. */

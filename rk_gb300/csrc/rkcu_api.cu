@@ -8,6 +8,7 @@
 #include <new>
 
 #include "rkcu.h"
+#include "rkcu_lowstorage.cuh"
 #include "rkcu_mixed.cuh"
 #include "rkcu_plain.cuh"
 
@@ -74,6 +75,9 @@ struct rkcu_solver {
   int stage_vectors = 0;
   float2 *mstage = nullptr;  // mixed form: f0, y32, S[2..s-1], dys, dyc, err
   int mstage_vectors = 0;
+  double2 *rings = nullptr;  // low-storage form: ring buffers
+  size_t ring_pairs = 0;
+  int ls_rows = 0;
   double *lv_r = nullptr, *lv_a = nullptr;
   DevState *st = nullptr;
   DevState *st_host = nullptr;  // pinned
@@ -124,6 +128,7 @@ int rkcu_destroy(rkcu_solver *s) {
   cudaFree(s->y[1]);
   cudaFree(s->stage);
   cudaFree(s->mstage);
+  cudaFree(s->rings);
   cudaFree(s->lv_r);
   cudaFree(s->lv_a);
   cudaFree(s->st);
@@ -146,7 +151,10 @@ int rkcu_create(rkcu_solver **out, const rkcu_problem *prob, const rkcu_options 
   if (o.precision != RKCU_FP64_EXACT && o.precision != RKCU_FP64_FMA && o.precision != RKCU_MIXED)
     return RKCU_ERR_INVALID;
   if (o.precision == RKCU_MIXED && prob->problem != RKCU_PROBLEM_BRUSS2D_MIX) return RKCU_ERR_INVALID;
-  if (o.variant != RKCU_VARIANT_D) return RKCU_ERR_INVALID;
+  if (o.variant != RKCU_VARIANT_D && o.variant != RKCU_VARIANT_LOWSTORAGE) return RKCU_ERR_INVALID;
+  if (o.variant == RKCU_VARIANT_LOWSTORAGE &&
+      (prob->problem != RKCU_PROBLEM_BRUSS2D_MIX || o.precision == RKCU_MIXED || o.block_rows < 0))
+    return RKCU_ERR_INVALID;
   if (o.step_limit < 0) return RKCU_ERR_INVALID;
   if (!(o.wait_timeout_s > 0.0)) o.wait_timeout_s = 10.0;
   if (!(o.h_init >= 0.0)) return RKCU_ERR_INVALID;
@@ -259,7 +267,29 @@ int rkcu_begin(rkcu_solver *s, double t0, double te, const double *y0, int y0_on
       s->dev_bytes += (long long)mneed * s->npairs * sizeof(float2);
     }
   }
-  const int need = s->opt.precision == RKCU_MIXED ? 0 : s->s + 1;  // w[1..s-1], dy, err
+  if (s->opt.variant == RKCU_VARIANT_LOWSTORAGE) {
+    const int N = s->prob.grid_n;
+    int R = s->opt.block_rows > 0 ? s->opt.block_rows : (s->s <= 8 ? 32 : 16);
+    if (R > N) R = N;
+    while (R > 1 && (double)R * N * N >= 1099511627776.0) R /= 2;  // row division needs q N < 2^40
+    const size_t need_pairs = rkcu::lowstorage_ring_pairs(s->s, R, N);
+    if (s->ring_pairs < need_pairs) {
+      if (s->rings) {
+        RKCU_CK(cudaStreamSynchronize(s->stream));
+        cudaFree(s->rings);
+        s->dev_bytes -= (long long)s->ring_pairs * sizeof(double2);
+        s->rings = nullptr;
+        s->ring_pairs = 0;
+      }
+      RKCU_CK(cudaMalloc(&s->rings, need_pairs * sizeof(double2)));
+      s->ring_pairs = need_pairs;
+      s->dev_bytes += (long long)need_pairs * sizeof(double2);
+    }
+    s->ls_rows = R;
+  }
+  const int need = (s->opt.precision == RKCU_MIXED || s->opt.variant == RKCU_VARIANT_LOWSTORAGE)
+                       ? 0
+                       : s->s + 1;  // w[1..s-1], dy, err
   if (s->stage_vectors < need) {
     if (s->stage) {
       RKCU_CK(cudaStreamSynchronize(s->stream));
@@ -300,6 +330,54 @@ int rkcu_advance(rkcu_solver *s, int max_steps) {
   if (!s->begun) return RKCU_ERR_STATE;
   if (max_steps <= 0) return RKCU_OK;
   RKCU_CK(cudaSetDevice(s->opt.device));
+  if (s->opt.variant == RKCU_VARIANT_LOWSTORAGE) {
+    rkcu::LsParams q;
+    std::memset(&q, 0, sizeof(q));
+    const int N = s->prob.grid_n, R = s->ls_rows;
+    q.N = N;
+    q.R = R;
+    q.nb = (N + R - 1) / R;
+    q.inv_n = (1ull << 40) / (unsigned long long)N + 1ull;
+    q.s = s->s;
+    q.ord = s->ord;
+    q.step_limit = s->opt.step_limit;
+    q.budget = max_steps;
+    q.extra_arrivals = s->extra_arrivals;
+    q.te = s->te;
+    q.tol = s->tol;
+    q.timeout_ns = (unsigned long long)(s->opt.wait_timeout_s * 1e9);
+    for (int i = 0; i < kMaxStages * kMaxStages; ++i) {
+      q.A[i] = s->A[i];
+      q.nzA[i] = s->A[i] != 0.0;
+    }
+    for (int i = 0; i < kMaxStages; ++i) {
+      q.b[i] = s->b[i];
+      q.bh[i] = s->bh[i];
+      q.nzb[i] = s->b[i] != 0.0;
+      q.nzbh[i] = s->bh[i] != 0.0;
+    }
+    q.y[0] = s->y[0];
+    q.y[1] = s->y[1];
+    const size_t blk = (size_t)R * N;
+    double2 *p = s->rings;
+    for (int l = 1; l < s->s; ++l) {
+      q.ring[l] = p;
+      p += (size_t)(2 * l + 2) * blk;
+    }
+    q.dyring = p;
+    p += (size_t)(2 * s->s - 1) * blk;
+    q.errring = p;
+    q.st = s->st;
+    q.bruss.N = N;
+    q.bruss.coef = bruss_coef(&s->prob);
+    int grid = 0;
+    cudaError_t e = rkcu::launch_lowstorage(q, s->opt.precision == RKCU_FP64_EXACT, s->num_sms,
+                                            s->stream, &grid);
+    if (e != cudaSuccess) return cuda_fail(e, "low-storage kernel launch");
+    s->last_grid = grid;
+    ++s->launches;
+    return RKCU_OK;
+  }
   if (s->opt.precision == RKCU_MIXED) {
     rkcu::MixedParams m;
     std::memset(&m, 0, sizeof(m));

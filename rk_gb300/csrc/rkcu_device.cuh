@@ -68,12 +68,25 @@ struct Bruss {
 
   template <bool kExact>
   __device__ __forceinline__ double2 eval(const double2 *__restrict__ w, int p) const {
-    using M = Arith<kExact>;
     const int k = p / N;
     const int j = p - k * N;
-    const double2 c = w[p];
-    const double2 up = w[k == 0 ? p + N : p - N];
-    const double2 dn = w[k == N - 1 ? p - N : p + N];
+    const double2 *row = w + (p - j);
+    return eval_rows<kExact>(k == 0 ? row + N : row - N, row, k == N - 1 ? row - N : row + N, j);
+  }
+
+  // Same, given the grid rows above (`up`: row k-1, or row k+1 on the first row),
+  // at (`cr`: row k) and below (`dn`: row k+1, or row k-1 on the last row) of the
+  // point, each indexed by column; lets stage vectors live in ring buffers.
+  template <bool kExact>
+  __device__ __forceinline__ double2 eval_rows(const double2 *__restrict__ upr,
+                                               const double2 *__restrict__ cr,
+                                               const double2 *__restrict__ dnr, int j) const {
+    using M = Arith<kExact>;
+    const double2 c = cr[j];
+    const double2 up = upr[j];
+    const double2 dn = dnr[j];
+    const double2 *w = cr;
+    const int p = j;
     double lu = M::add(up.x, dn.x);
     double lv = M::add(up.y, dn.y);
     if (j == 0) {

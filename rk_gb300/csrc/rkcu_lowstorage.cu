@@ -1,0 +1,269 @@
+// Low-storage form of the step loop for BRUSS2D-MIX (the GPU counterpart of
+// the reference's pipelined low-storage variant, src/impl/seq/PipeDls.c:49-131).
+//
+// The grid's rows are cut into nb blocks of R rows (a block is at least the
+// access distance, one row = 2N components).  One RK step is a wavefront of
+// nb + 2(s-1) steps tau; at wavefront step tau, stage i works on block
+// b = tau - 2i.  With this skew of two, everything stage i reads on blocks
+// b-1, b, b+1 was completed at an earlier tau, and no stage reads a block
+// another stage writes at the same tau, so one grid barrier per tau suffices
+// and all stages of a wavefront step run concurrently.
+//
+// Storage: y (two full vectors, ping-pong as in the plain form) plus ring
+// buffers: w_l keeps the blocks from tau-2l-1 to tau (2l+2 slots), dy and err
+// keep 2s-1 blocks -- 2n + (s^2 + 5s - 4) R 2N doubles instead of (s+3) n;
+// for N = 2000, R = 32, DOPRI5(4): 128 MB + 82 MB instead of 640 MB, and the
+// window stays in L2.  Every component sees the same operations in the same
+// order as in the plain form, so results are bit-identical to it.
+#include "rkcu.h"
+#include "rkcu_lowstorage.cuh"
+
+namespace rkcu {
+
+constexpr int kLsThreads = 256;
+
+template <bool kExact>
+__global__ void __launch_bounds__(kLsThreads) ls_kernel(const __grid_constant__ LsParams P) {
+  using M = Arith<kExact>;
+  __shared__ double hA[kMaxStages * kMaxStages];
+  __shared__ double hb[kMaxStages], hbh[kMaxStages];
+  __shared__ double s_t, s_h, s_pend_err, s_pend_h;
+  __shared__ int s_acc, s_rej, s_cur, s_done, s_pending;
+  __shared__ unsigned long long s_step;
+  __shared__ double s_wmax[kLsThreads / 32];
+  __shared__ int s_start[kMaxStages + 1], s_stage[kMaxStages], s_nact;
+
+  DevState *st = P.st;
+  const int s = P.s, N = P.N, R = P.R, nb = P.nb;
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gstride = gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const size_t blk = static_cast<size_t>(R) * N;  // pairs per block slot
+
+  if (threadIdx.x == 0) {
+    s_t = st->t;
+    s_h = st->h;
+    s_acc = st->steps_acc;
+    s_rej = st->steps_rej;
+    s_cur = st->cur;
+    s_done = st->done;
+    s_step = st->step;
+    s_pending = st->pending;
+    s_pend_err = st->pend_err;
+    s_pend_h = st->pend_h;
+  }
+  __syncthreads();
+
+  bool ok = true;
+  for (int it = 0; it < P.budget; ++it) {
+    if (s_done || s_pending) break;
+    const double h = s_h;
+    for (int idx = threadIdx.x; idx < kMaxStages * kMaxStages; idx += blockDim.x)
+      hA[idx] = h * P.A[idx];
+    if (threadIdx.x < kMaxStages) {
+      hb[threadIdx.x] = h * P.b[threadIdx.x];
+      hbh[threadIdx.x] = h * P.bh[threadIdx.x];
+    }
+    __syncthreads();
+    const double2 *__restrict__ ycur = P.y[s_cur];
+    double2 *__restrict__ ynew = P.y[s_cur ^ 1];
+    double emax = 0.0;
+
+    const int ntau = nb + 2 * (s - 1);
+    for (int tau = 0; tau < ntau && ok; ++tau) {
+      // the stages active at this wavefront step and where their items start
+      if (threadIdx.x == 0) {
+        int cnt = 0, off = 0;
+        for (int i = 0; i < s; ++i) {
+          const int b = tau - 2 * i;
+          if (b < 0 || b >= nb) continue;
+          const int rows = min(R, N - b * R);
+          s_stage[cnt] = i;
+          s_start[cnt] = off;
+          off += rows * N;
+          ++cnt;
+        }
+        s_start[cnt] = off;
+        s_nact = cnt;
+      }
+      __syncthreads();
+      const int nact = s_nact;
+      const int total = s_start[nact];
+      for (int u = gtid; u < total; u += gstride) {
+        int a = 0;
+        while (a + 1 < nact && u >= s_start[a + 1]) ++a;
+        const int i = s_stage[a];
+        const int b = tau - 2 * i;
+        const int q = u - s_start[a];
+        const int r = static_cast<int>((static_cast<unsigned long long>(q) * P.inv_n) >> 40);
+        const int j = q - r * N;
+        const int k = b * R + r;  // grid row
+        // argument vector rows: y for stage 0, the ring of w_i otherwise
+        const double2 *upr, *cr, *dnr;
+        const int ku = (k == 0) ? k + 1 : k - 1;
+        const int kd = (k == N - 1) ? k - 1 : k + 1;
+        if (i == 0) {
+          cr = ycur + static_cast<size_t>(k) * N;
+          upr = ycur + static_cast<size_t>(ku) * N;
+          dnr = ycur + static_cast<size_t>(kd) * N;
+        } else {
+          const int m = 2 * i + 2;
+          const double2 *ring = P.ring[i];
+          const int bu = ku / R, bd = kd / R;  // R is at least 1; blocks b-1..b+1
+          cr = ring + static_cast<size_t>(b % m) * blk + static_cast<size_t>(r) * N;
+          upr = ring + static_cast<size_t>(bu % m) * blk + static_cast<size_t>(ku - bu * R) * N;
+          dnr = ring + static_cast<size_t>(bd % m) * blk + static_cast<size_t>(kd - bd * R) * N;
+        }
+        const double2 F = P.bruss.eval_rows<kExact>(upr, cr, dnr, j);
+        const size_t loc = static_cast<size_t>(r) * N + j;  // position inside a block slot
+        const int md = 2 * s - 1;
+        double2 *dyp = P.dyring + static_cast<size_t>(b % md) * blk + loc;
+        double2 *erp = P.errring + static_cast<size_t>(b % md) * blk + loc;
+        if (i == 0) {
+          const double2 Y = cr[j];
+          for (int l = 1; l < s; ++l) {
+            double2 wv = Y;
+            if (P.nzA[l * kMaxStages]) {
+              const double aa = hA[l * kMaxStages];
+              wv.x = M::mac(Y.x, aa, F.x);
+              wv.y = M::mac(Y.y, aa, F.y);
+            }
+            P.ring[l][static_cast<size_t>(b % (2 * l + 2)) * blk + loc] = wv;
+          }
+          *dyp = make_double2(M::mul(hb[0], F.x), M::mul(hb[0], F.y));
+          *erp = make_double2(M::mul(hbh[0], F.x), M::mul(hbh[0], F.y));
+        } else {
+          double2 dd = *dyp, e = *erp;
+          if (P.nzb[i]) {
+            dd.x = M::mac(dd.x, hb[i], F.x);
+            dd.y = M::mac(dd.y, hb[i], F.y);
+          }
+          if (P.nzbh[i]) {
+            e.x = M::mac(e.x, hbh[i], F.x);
+            e.y = M::mac(e.y, hbh[i], F.y);
+          }
+          if (i < s - 1) {
+            for (int l = i + 1; l < s; ++l) {
+              if (!P.nzA[l * kMaxStages + i]) continue;
+              const double aa = hA[l * kMaxStages + i];
+              double2 *wl = P.ring[l] + static_cast<size_t>(b % (2 * l + 2)) * blk + loc;
+              double2 wv = *wl;
+              wv.x = M::mac(wv.x, aa, F.x);
+              wv.y = M::mac(wv.y, aa, F.y);
+              *wl = wv;
+            }
+            *dyp = dd;
+            *erp = e;
+          } else {
+            const size_t g = static_cast<size_t>(k) * N + j;
+            const double2 Y = ycur[g];
+            const double2 yn = make_double2(M::add(Y.x, dd.x), M::add(Y.y, dd.y));
+            ynew[g] = yn;
+            double dv = fmax(fabs(yn.x), fabs(Y.x));
+            emax = fmax(emax, dv == 0.0 ? 1.7E308 : fabs(e.x) / dv);
+            dv = fmax(fabs(yn.y), fabs(Y.y));
+            emax = fmax(emax, dv == 0.0 ? 1.7E308 : fabs(e.y) / dv);
+          }
+        }
+      }
+      ok = grid_barrier(st, P.nblocks, P.timeout_ns, 30);
+    }
+    if (!ok) break;
+
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) emax = fmax(emax, __shfl_xor_sync(0xffffffffu, emax, off));
+    if (lane == 0) s_wmax[warp] = emax;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double mm = s_wmax[0];
+      for (int k = 1; k < kLsThreads / 32; ++k) mm = fmax(mm, s_wmax[k]);
+      atomicMax(&st->err_slot[s_step & 1], (unsigned long long)__double_as_longlong(mm));
+    }
+    if (!(ok = grid_barrier(st, P.nblocks, P.timeout_ns, 31))) break;
+
+    // step control: as in the plain form (tools.h:191-198, 235-278)
+    if (threadIdx.x == 0) {
+      if (blockIdx.x == 0) st->err_slot[(s_step + 1) & 1] = 0ull;
+      const double errmax =
+          __longlong_as_double((long long)*(volatile unsigned long long *)&st->err_slot[s_step & 1]);
+      double t = s_t, hh = s_h;
+      int acc = s_acc, rej = s_rej, cur = s_cur;
+      bool host_pow = false;
+      if (P.tol <= 0.0) {
+        t += hh;
+        ++acc;
+        cur ^= 1;
+      } else {
+        const double hn = h_new(hh, errmax, P.tol, P.ord, &host_pow);
+        if (errmax <= P.tol) {
+          t += hh;
+          ++acc;
+          cur ^= 1;
+        } else {
+          ++rej;
+        }
+        if (host_pow) {
+          s_pend_err = errmax;
+          s_pend_h = hh;
+        } else {
+          hh = hn;
+        }
+      }
+      s_pending = host_pow;
+      if (!host_pow) {
+        hh = fmin(hh, P.te - t);
+        s_done = !(t < P.te) || (P.step_limit > 0 && acc + rej >= P.step_limit);
+      }
+      s_t = t;
+      s_h = hh;
+      s_acc = acc;
+      s_rej = rej;
+      s_cur = cur;
+      s_step = s_step + 1;
+    }
+    __syncthreads();
+    if (s_pending) break;
+  }
+
+  if (ok && blockIdx.x == 0 && threadIdx.x == 0) {
+    st->t = s_t;
+    st->h = s_h;
+    st->steps_acc = s_acc;
+    st->steps_rej = s_rej;
+    st->cur = s_cur;
+    st->done = s_done;
+    st->step = s_step;
+    st->pending = s_pending;
+    st->pend_err = s_pend_err;
+    st->pend_h = s_pend_h;
+  }
+}
+
+template <bool kExact>
+static cudaError_t launch_t(const LsParams &p, int num_sms, cudaStream_t stream, int *grid_out) {
+  int occ = 0;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ls_kernel<kExact>, kLsThreads, 0);
+  if (e != cudaSuccess) return e;
+  if (occ < 1) return cudaErrorInvalidConfiguration;
+  int grid = occ * num_sms;
+  LsParams q = p;
+  q.nblocks = grid + (p.extra_arrivals > 0 ? p.extra_arrivals : 0);
+  void *args[] = {&q};
+  *grid_out = grid;
+  return cudaLaunchCooperativeKernel((const void *)ls_kernel<kExact>, dim3(grid), dim3(kLsThreads),
+                                     args, 0, stream);
+}
+
+cudaError_t launch_lowstorage(const LsParams &p, bool exact, int num_sms, cudaStream_t stream,
+                              int *grid_out) {
+  return exact ? launch_t<true>(p, num_sms, stream, grid_out)
+               : launch_t<false>(p, num_sms, stream, grid_out);
+}
+
+size_t lowstorage_ring_pairs(int s, int R, int N) {
+  size_t slots = 2 * (2 * static_cast<size_t>(s) - 1);
+  for (int l = 1; l < s; ++l) slots += 2 * static_cast<size_t>(l) + 2;
+  return slots * static_cast<size_t>(R) * N;
+}
+
+}  // namespace rkcu

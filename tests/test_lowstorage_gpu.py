@@ -1,0 +1,48 @@
+"""Low-storage (pipelined wavefront) variant: bit-identical to the reference and
+to the plain form for any block size, with 2n + O(s^2 B) device storage."""
+import hashlib
+
+import numpy as np
+import pytest
+
+import rk_gb300 as rk
+from conftest import all_golden, golden_y, golden_y0, load_golden
+
+pytestmark = pytest.mark.gpu
+
+CASES = [g for g in all_golden() if g["problem"] == "bruss2d-mix" and g["n"] * g["steps"] <= 5e9]
+
+
+def _solve(rec, rows, precision="exact"):
+    with rk.Solver(rk.bruss2d_mix(rec["grid_n"], rec["alpha"]), method=rec["method"],
+                   precision=precision, step_limit=rec["step_limit"],
+                   variant=rk.VARIANT_LOWSTORAGE, block_rows=rows) as s:
+        y, st = s.solve(rec["t0"], rec["t_end"], golden_y0(rec), rec["tol"])
+        return y, st, s.device_bytes
+
+
+@pytest.mark.parametrize("rows", [0, 1, 3])
+@pytest.mark.parametrize("rec", CASES, ids=[g["name"] for g in CASES])
+def test_lowstorage_bit_identical_to_reference(rec, rows):
+    y, st, _ = _solve(rec, rows)
+    assert (st["steps_acc"], st["steps_rej"]) == (rec["accepted"], rec["rejected"])
+    idx, ref = golden_y(rec)
+    np.testing.assert_array_equal(y[idx], ref)
+    assert hashlib.sha256(y.astype("<f8").tobytes()).hexdigest() == rec["y_sha256"]
+
+
+def test_lowstorage_n2000_matches_reference_with_less_memory():
+    rec = load_golden("bruss_n2000_dopri54_tol1e-6")
+    y, st, ls_bytes = _solve(rec, 0)
+    assert (st["steps_acc"], st["steps_rej"]) == (rec["accepted"], rec["rejected"])
+    assert hashlib.sha256(y.astype("<f8").tobytes()).hexdigest() == rec["y_sha256"]
+    n = rec["n"]
+    # 2n state doubles + the ring window, far below the plain form's (s+3) n
+    assert ls_bytes < 0.4 * (7 + 3) * n * 8
+    print(f"low-storage device bytes {ls_bytes / 1e6:.0f} MB vs plain {(7 + 3) * n * 8 / 1e6:.0f} MB")
+
+
+def test_lowstorage_rejects_other_problems():
+    with pytest.raises(rk.RkcuError) as ei:
+        rk.Solver(rk.lv_pairs(10), variant=rk.VARIANT_LOWSTORAGE)
+    assert ei.value.status == rk.ERR_INVALID
