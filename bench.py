@@ -211,7 +211,9 @@ def run_ours(args):
     torch.cuda.synchronize()
 
     solver = rk.Solver(prob, method=args.method, precision=args.precision, device=local,
-                       stream=stream.cuda_stream)
+                       stream=stream.cuda_stream,
+                       variant=rk.VARIANT_LOWSTORAGE if args.variant == "lowstorage" else rk.VARIANT_D,
+                       block_rows=args.block_rows)
     # ---- device-resident timing -------------------------------------------
     solver.begin(T0, TE, None, TOL, y0_device_ptr=y0_dev.data_ptr())
     st0 = solver.run(args.warmup)
@@ -278,7 +280,7 @@ def run_ours(args):
         "data": "synthetic (ode_start initial values of BRUSS2D-MIX)",
         "config": {"workload": f"bruss2d-mix N={args.grid} n={n} {args.method} tol=1e-6 t=[0,0.5]",
                    "grid_n": args.grid, "alpha": ALPHA, "method": args.method,
-                   "precision": args.precision, "parallelism": f"replicas{ws}",
+                   "precision": args.precision, "variant": args.variant, "parallelism": f"replicas{ws}",
                    "l2": f"per-step working set {dev_bytes / 1e6:.0f} MB > {L2_BYTES / 1e6:.0f} MB L2, no flush"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
@@ -473,6 +475,9 @@ def run_served(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--workload", default="plain", choices=["plain", "batched", "served"])
+    ap.add_argument("--variant", default="d", choices=["d", "lowstorage"],
+                    help="d: stage vectors in HBM (default); lowstorage: wavefront with ring buffers")
+    ap.add_argument("--block-rows", type=int, default=0)
     ap.add_argument("--requests", type=int, default=400)
     ap.add_argument("--load", type=float, default=0.5)
     ap.add_argument("--arena-gb", type=float, default=8.0)
