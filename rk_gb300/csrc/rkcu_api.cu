@@ -81,6 +81,7 @@ struct rkcu_solver {
   double *lv_r = nullptr, *lv_a = nullptr;
   DevState *st = nullptr;
   DevState *st_host = nullptr;  // pinned
+  unsigned int *flags = nullptr;  // plain kernel: per-CTA stage progress
   // run
   bool begun = false;
   double te = 0.0, tol = 0.0;
@@ -132,6 +133,7 @@ int rkcu_destroy(rkcu_solver *s) {
   cudaFree(s->lv_r);
   cudaFree(s->lv_a);
   cudaFree(s->st);
+  cudaFree(s->flags);
   cudaFreeHost(s->st_host);
   if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
   delete s;
@@ -194,6 +196,8 @@ int rkcu_create(rkcu_solver **out, const rkcu_problem *prob, const rkcu_options 
     return fail(cuda_fail(e, "cudaMalloc state"));
   if ((e = cudaMallocHost(&s->st_host, sizeof(DevState))) != cudaSuccess)
     return fail(cuda_fail(e, "cudaMallocHost"));
+  if ((e = cudaMalloc(&s->flags, sizeof(unsigned int) * rkcu::kMaxPlainGrid)) != cudaSuccess)
+    return fail(cuda_fail(e, "cudaMalloc flags"));
   if (prob->problem == RKCU_PROBLEM_LV_BANDED) {
     const size_t np = 2 * s->npairs;
     if ((e = cudaMalloc(&s->lv_r, np * sizeof(double))) != cudaSuccess)
@@ -451,6 +455,7 @@ int rkcu_advance(rkcu_solver *s, int max_steps) {
   p.dy = s->stage + (size_t)(s->s - 1) * s->npairs;
   p.err = s->stage + (size_t)s->s * s->npairs;
   p.st = s->st;
+  p.flags = s->flags;
   p.bruss.N = s->prob.grid_n;
   p.bruss.coef = s->prob.problem == RKCU_PROBLEM_BRUSS2D_MIX ? bruss_coef(&s->prob) : 0.0;
   p.lvb.n = s->prob.n;

@@ -65,6 +65,8 @@ struct Arith<false> {
 struct Bruss {
   int N;        // grid size
   double coef;  // (alpha * (N-1)) * (N-1), evaluated on the host in that order
+  // pairs on either side a point's stencil reaches: one grid row (ode_acc_dist = 2N components)
+  __device__ __forceinline__ int dep_pairs() const { return N; }
 
   template <bool kExact>
   __device__ __forceinline__ double2 eval(const double2 *__restrict__ w, int p) const {
@@ -115,6 +117,7 @@ struct Bruss {
 // LV pairs (src/problems/lv.c:66-87):
 //   prey  f0 = c0*y0 - d0*y0*y1,  predator f1 = d1*y0*y1 - c1*y1
 struct LvPairs {
+  __device__ __forceinline__ int dep_pairs() const { return 0; }
   template <bool kExact>
   __device__ __forceinline__ double2 eval(const double2 *__restrict__ w, int p) const {
     using M = Arith<kExact>;
@@ -131,6 +134,7 @@ struct LvBanded {
   int n;
   const double *__restrict__ r;  // r[n_pad]
   const double *__restrict__ a;  // a[n_pad][5]
+  __device__ __forceinline__ int dep_pairs() const { return 1; }
 
   template <bool kExact>
   __device__ __forceinline__ double comp(const double *__restrict__ y, int i) const {
@@ -215,6 +219,82 @@ __device__ __forceinline__ bool grid_barrier(DevState *st, unsigned int nblocks,
     }
     __threadfence();
     s_ok = ok && (*(volatile int *)&st->error == 0);
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// Per-thread maximum of |e| / max(|y_new|, |y_old|) (include/tools.h:280-288)
+// with an FP64 division only for components that can be the maximum.  The high
+// word of a positive double, (exponent << 20) | top mantissa bits, is 2^20
+// (log2 x + 1023) to within 0.086 * 2^20, so hi(|e|) - hi(divisor) estimates
+// 2^20 log2(ratio) to within 0.18 * 2^20; a component whose estimate is more
+// than kMargin below the key of the current exact maximum cannot exceed it.
+// Zero divisors, infinities and NaNs take the exact path, so the result is the
+// reference's (a zero divisor gives 1.7E308, a NaN ratio is ignored by fmax).
+struct ErrMax {
+  static constexpr int kMargin = 1 << 19;  // 0.5 in log2 units
+  double best = 0.0;
+  int best_key = -0x40000000;
+
+  __device__ __forceinline__ void add(double e, double yn, double yo) {
+    const long long ae = __double_as_longlong(e) & 0x7fffffffffffffffLL;
+    const long long an = __double_as_longlong(yn) & 0x7fffffffffffffffLL;
+    const long long ao = __double_as_longlong(yo) & 0x7fffffffffffffffLL;
+    constexpr long long kInf = 0x7ff0000000000000LL;
+    constexpr long long kMinNormal = 0x0010000000000000LL;
+    const long long d = an > ao ? an : ao;
+    // a subnormal or zero divisor would make the estimate too low: exact path
+    const bool special = ae >= kInf || an > kInf || ao > kInf || d < kMinNormal;
+    const int key = static_cast<int>(ae >> 32) - static_cast<int>(d >> 32);
+    if (special || key > best_key - kMargin) {
+      const double div = fmax(fabs(yn), fabs(yo));
+      const double r = div == 0.0 ? 1.7E308 : fabs(e) / div;
+      if (r > best) {  // false for NaN, as fmax would ignore it
+        best = r;
+        best_key = static_cast<int>(__double_as_longlong(r) >> 32) - 0x3ff00000;
+      }
+    }
+  }
+};
+
+// Neighbour synchronisation for the plain step loop: each CTA publishes how
+// many stages it has completed in this launch; a CTA starts a stage once the
+// CTAs whose pairs its stencil reads have completed the previous one.
+__device__ __forceinline__ void publish_progress(unsigned int *flags, unsigned int value) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicExch(&flags[blockIdx.x], value);
+  }
+}
+
+__device__ __forceinline__ bool wait_neighbours(const unsigned int *flags, int c_lo, int c_hi,
+                                                unsigned int target, DevState *st,
+                                                unsigned long long timeout_ns, int site) {
+  __shared__ int s_ok;
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    const unsigned long long t0 = globaltimer_ns();
+    for (int c = c_lo; c <= c_hi && ok; ++c) {
+      if (c == static_cast<int>(blockIdx.x)) continue;
+      unsigned int ns = 32;
+      while (*(volatile const unsigned int *)&flags[c] < target) {
+        if (*(volatile int *)&st->error) {
+          ok = 0;
+          break;
+        }
+        if (globaltimer_ns() - t0 > timeout_ns) {
+          if (atomicCAS(&st->error, 0, 1) == 0) st->error_site = site;
+          ok = 0;
+          break;
+        }
+        __nanosleep(ns);
+        if (ns < 256) ns <<= 1;
+      }
+    }
+    __threadfence();
+    s_ok = ok;
   }
   __syncthreads();
   return s_ok != 0;

@@ -27,8 +27,10 @@ constexpr int kNoAllocMaxComponents = 1 << 16;
 constexpr size_t kPairs = kNoAllocMaxComponents / 2;
 // y[2], w[1..s-1] (at most kMaxStages-1), dy, err
 constexpr size_t kVectors = 2 + (kMaxStages - 1) + 2;
-// the step-control state occupies the first 256 bytes
+// the step-control state occupies the first 256 bytes, the plain kernel's
+// per-CTA progress words the next kMaxPlainGrid * 4 bytes
 constexpr size_t kStatePairs = 16;
+constexpr size_t kFlagPairs = rkcu::kMaxPlainGrid * sizeof(unsigned int) / sizeof(double2);
 static_assert(sizeof(DevState) <= kStatePairs * sizeof(double2), "state does not fit");
 
 constexpr int kMaxDevices = 64;
@@ -37,8 +39,8 @@ std::mutex g_setup_mutex;
 
 }  // namespace
 
-// 8 MiB + 256 B per device: all scratch of rkcu_solve_noalloc.
-static __device__ __align__(256) double2 g_noalloc_scratch[kStatePairs + kVectors * kPairs];
+// 8 MiB + 8.25 KiB per device: all scratch of rkcu_solve_noalloc.
+static __device__ __align__(256) double2 g_noalloc_scratch[kStatePairs + kFlagPairs + kVectors * kPairs];
 
 namespace {
 
@@ -99,7 +101,8 @@ extern "C" int rkcu_solve_noalloc(const rkcu_problem *prob, const char *method, 
 
   const int npairs = prob->n / 2;
   DevState *dstate = reinterpret_cast<DevState *>(scratch);
-  double2 *vec = scratch + kStatePairs;
+  unsigned int *flags = reinterpret_cast<unsigned int *>(scratch + kStatePairs);
+  double2 *vec = scratch + kStatePairs + kFlagPairs;
   rkcu::PlainParams p;
   std::memset(&p, 0, sizeof(p));
   p.npairs = npairs;
@@ -127,6 +130,7 @@ extern "C" int rkcu_solve_noalloc(const rkcu_problem *prob, const char *method, 
   p.dy = vec + (size_t)(1 + s) * kPairs;
   p.err = vec + (size_t)(2 + s) * kPairs;
   p.st = dstate;
+  p.flags = flags;
   p.bruss.N = prob->grid_n;
   if (prob->problem == RKCU_PROBLEM_BRUSS2D_MIX) {
     const double n1 = static_cast<double>(prob->grid_n) - 1.0;

@@ -10,10 +10,13 @@
 //                   the reference's y_old restore copy (tools.h:273) is not needed
 //   w[1..s-1]       stage arguments, accumulated in scatter order
 //   dy, err         the b- and (b - b_hat)-weighted sums
-// Each stage is one grid-stride sweep over the pairs followed by a bounded grid
-// barrier (the stencil of the next stage reads neighbours written by other
-// CTAs).  The error max is reduced by warp shuffles, shared memory and one
-// 64-bit atomicMax per CTA on the bit pattern (the values are >= 0).
+// Every CTA owns one contiguous range of pairs (block distribution as
+// src/tools.c:42-56).  Between stages a CTA waits only for the CTAs whose
+// pairs its stencil reads (one grid row either side for BRUSS2D-MIX) to
+// publish the previous stage; one bounded grid barrier per step closes the
+// last stage before the error max is read.  The error max is reduced by warp
+// shuffles, shared memory and one 64-bit atomicMax per CTA on the bit pattern
+// (the values are >= 0).
 #include "rkcu_plain.cuh"
 #include "rkcu.h"
 
@@ -30,12 +33,6 @@ __device__ __forceinline__ const LvPairs &problem_of<LvPairs>(const PlainParams 
 template <>
 __device__ __forceinline__ const LvBanded &problem_of<LvBanded>(const PlainParams &P) { return P.lvb; }
 
-// |e| / max(|y_new|, |y_old|), with the reference's 1.7E308 for a zero divisor
-__device__ __forceinline__ double err_ratio(double e, double yn, double yo) {
-  const double div = fmax(fabs(yn), fabs(yo));
-  return div == 0.0 ? 1.7E308 : fabs(e) / div;
-}
-
 template <class Prob, bool kExact>
 __global__ void __launch_bounds__(kThreads) plain_kernel(const __grid_constant__ PlainParams P) {
   using M = Arith<kExact>;
@@ -50,8 +47,6 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(const __grid_constant__
   const Prob &prob = problem_of<Prob>(P);
   DevState *st = P.st;
   const int s = P.s;
-  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int gstride = gridDim.x * blockDim.x;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
   if (threadIdx.x == 0) {
@@ -67,6 +62,18 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(const __grid_constant__
     s_pend_h = st->pend_h;
   }
   __syncthreads();
+
+  // this CTA's pairs [lo, hi) and the CTAs whose pairs its stencil reads
+  const int G = gridDim.x;
+  const int q = P.npairs / G, rr = P.npairs % G;
+  const int bx = blockIdx.x;
+  const int lo = bx < rr ? bx * (q + 1) : rr * (q + 1) + (bx - rr) * q;
+  const int hi = lo + (bx < rr ? q + 1 : q);
+  const int dep = prob.dep_pairs();
+  auto owner = [&](int p) { return p < rr * (q + 1) ? p / (q + 1) : rr + (p - rr * (q + 1)) / max(q, 1); };
+  const int c_lo = owner(max(0, lo - dep));
+  const int c_hi = owner(min(P.npairs - 1, max(lo, hi - 1) + dep));
+  unsigned int progress = 0;
 
   bool ok = true;
   for (int it = 0; it < P.budget; ++it) {
@@ -84,7 +91,7 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(const __grid_constant__
     double2 *__restrict__ ynew = P.y[s_cur ^ 1];
 
     // first stage (block-inline.h:253-272)
-    for (int p = gtid; p < P.npairs; p += gstride) {
+    for (int p = lo + threadIdx.x; p < hi; p += blockDim.x) {
       const double2 F = prob.template eval<kExact>(ycur, p);
       const double2 Y = ycur[p];
       for (int l = 1; l < s; ++l) {
@@ -99,14 +106,15 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(const __grid_constant__
       P.dy[p] = make_double2(M::mul(hb[0], F.x), M::mul(hb[0], F.y));
       P.err[p] = make_double2(M::mul(hbh[0], F.x), M::mul(hbh[0], F.y));
     }
-    if (!(ok = grid_barrier(st, P.nblocks, P.timeout_ns, 1))) break;
+    publish_progress(P.flags, ++progress);
+    if (!(ok = wait_neighbours(P.flags, c_lo, c_hi, progress, st, P.timeout_ns, 1))) break;
 
     // intermediate stages (block-inline.h:276-294)
     for (int i = 1; i < s - 1; ++i) {
       const double2 *__restrict__ wi = P.w[i];
       const double bi = hb[i], bhi = hbh[i];
       const bool nzb = P.nzb[i], nzbh = P.nzbh[i];
-      for (int p = gtid; p < P.npairs; p += gstride) {
+      for (int p = lo + threadIdx.x; p < hi; p += blockDim.x) {
         const double2 F = prob.template eval<kExact>(wi, p);
         for (int l = i + 1; l < s; ++l) {
           if (!P.nzA[l * kMaxStages + i]) continue;
@@ -129,18 +137,19 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(const __grid_constant__
           P.err[p] = e;
         }
       }
-      if (!(ok = grid_barrier(st, P.nblocks, P.timeout_ns, 2))) break;
+      publish_progress(P.flags, ++progress);
+      if (!(ok = wait_neighbours(P.flags, c_lo, c_hi, progress, st, P.timeout_ns, 2))) break;
     }
     if (!ok) break;
 
     // last stage (block-inline.h:298-320) and error max (tools.h:280-288)
-    double emax = 0.0;
+    ErrMax em;
     {
       const int i = s - 1;
       const double2 *__restrict__ wl = P.w[i];
       const double bi = hb[i], bhi = hbh[i];
       const bool nzb = P.nzb[i], nzbh = P.nzbh[i];
-      for (int p = gtid; p < P.npairs; p += gstride) {
+      for (int p = lo + threadIdx.x; p < hi; p += blockDim.x) {
         const double2 F = prob.template eval<kExact>(wl, p);
         double2 d = P.dy[p];
         double2 e = P.err[p];
@@ -155,10 +164,11 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(const __grid_constant__
         const double2 Y = ycur[p];
         const double2 yn = make_double2(M::add(Y.x, d.x), M::add(Y.y, d.y));
         ynew[p] = yn;
-        emax = fmax(emax, err_ratio(e.x, yn.x, Y.x));
-        if (2 * p + 1 < P.n) emax = fmax(emax, err_ratio(e.y, yn.y, Y.y));
+        em.add(e.x, yn.x, Y.x);
+        if (2 * p + 1 < P.n) em.add(e.y, yn.y, Y.y);
       }
     }
+    double emax = em.best;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) emax = fmax(emax, __shfl_xor_sync(0xffffffffu, emax, off));
     if (lane == 0) s_wmax[warp] = emax;
@@ -248,10 +258,13 @@ static cudaError_t launch_one(const PlainParams &p, int blocks_per_sm, int num_s
   int grid = per_sm * num_sms;
   const int useful = (p.npairs + kThreads - 1) / kThreads;
   if (grid > useful) grid = useful > 0 ? useful : 1;
+  if (grid > kMaxPlainGrid) grid = kMaxPlainGrid;
   PlainParams q = p;
   q.nblocks = grid + (p.extra_arrivals > 0 ? p.extra_arrivals : 0);
   void *args[] = {&q};
   *grid_out = grid;
+  e = cudaMemsetAsync(p.flags, 0, sizeof(unsigned int) * grid, stream);
+  if (e != cudaSuccess) return e;
   return cudaLaunchCooperativeKernel((const void *)kern, dim3(grid), dim3(kThreads), args, 0,
                                      stream);
 }

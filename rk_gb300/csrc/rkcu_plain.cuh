@@ -27,10 +27,14 @@ struct PlainParams {
   double2 *w[kMaxStages];             // w[1..s-1]
   double2 *dy, *err;
   DevState *st;
+  unsigned int *flags;                // kMaxPlainGrid progress words (reset by each launch)
   Bruss bruss;
   LvPairs lvp;
   LvBanded lvb;
 };
+
+// Largest grid the plain kernel uses (the progress words are sized for it).
+constexpr int kMaxPlainGrid = 2048;
 
 // Launches one persistent kernel (cooperative) for up to p.budget steps.
 cudaError_t launch_plain(const PlainParams &p, bool exact, int blocks_per_sm, int num_sms,
