@@ -79,6 +79,8 @@ typedef struct
                            (pass the reference's own initial_stepsize() result or H_INIT) */
   int block_rows;       /* RKCU_VARIANT_LOWSTORAGE: grid rows per pipeline block (the
                            reference's BLOCKSIZE in rows, config.h:97-98); 0 = automatic */
+  int schedule;         /* plain form, stage synchronisation: 0 = automatic, 1 = grid
+                           barrier after every stage, 2 = neighbour progress flags */
 } rkcu_options;
 
 /* Progress of a solve: the counters of src/tools.c:62-79 plus the current t, h. */

@@ -160,6 +160,7 @@ int rkcu_create(rkcu_solver **out, const rkcu_problem *prob, const rkcu_options 
   if (o.step_limit < 0) return RKCU_ERR_INVALID;
   if (!(o.wait_timeout_s > 0.0)) o.wait_timeout_s = 10.0;
   if (!(o.h_init >= 0.0)) return RKCU_ERR_INVALID;
+  if (o.schedule < 0 || o.schedule > 2) return RKCU_ERR_INVALID;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= o.device || o.device < 0)
     return RKCU_ERR_NO_DEVICE;
@@ -456,6 +457,7 @@ int rkcu_advance(rkcu_solver *s, int max_steps) {
   p.err = s->stage + (size_t)s->s * s->npairs;
   p.st = s->st;
   p.flags = s->flags;
+  p.schedule = s->opt.schedule == 2 ? rkcu::kScheduleNeighbour : rkcu::kScheduleGrid;
   p.bruss.N = s->prob.grid_n;
   p.bruss.coef = s->prob.problem == RKCU_PROBLEM_BRUSS2D_MIX ? bruss_coef(&s->prob) : 0.0;
   p.lvb.n = s->prob.n;

@@ -131,6 +131,7 @@ extern "C" int rkcu_solve_noalloc(const rkcu_problem *prob, const char *method, 
   p.err = vec + (size_t)(2 + s) * kPairs;
   p.st = dstate;
   p.flags = flags;
+  p.schedule = rkcu::kScheduleGrid;
   p.bruss.N = prob->grid_n;
   if (prob->problem == RKCU_PROBLEM_BRUSS2D_MIX) {
     const double n1 = static_cast<double>(prob->grid_n) - 1.0;

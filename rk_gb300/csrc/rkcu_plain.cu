@@ -33,6 +33,15 @@ __device__ __forceinline__ const LvPairs &problem_of<LvPairs>(const PlainParams 
 template <>
 __device__ __forceinline__ const LvBanded &problem_of<LvBanded>(const PlainParams &P) { return P.lvb; }
 
+// Between stages: either the CTAs whose pairs this CTA's stencil reads have
+// published the stage (neighbour flags), or every CTA has (grid barrier).
+__device__ __forceinline__ bool stage_sync(const PlainParams &P, int c_lo, int c_hi,
+                                           unsigned int progress, int site) {
+  if (P.schedule == kScheduleGrid) return grid_barrier(P.st, P.nblocks, P.timeout_ns, site);
+  publish_progress(P.flags, progress);
+  return wait_neighbours(P.flags, c_lo, c_hi, progress, P.st, P.timeout_ns, site);
+}
+
 template <class Prob, bool kExact>
 __global__ void __launch_bounds__(kThreads) plain_kernel(const __grid_constant__ PlainParams P) {
   using M = Arith<kExact>;
@@ -69,6 +78,11 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(const __grid_constant__
   const int bx = blockIdx.x;
   const int lo = bx < rr ? bx * (q + 1) : rr * (q + 1) + (bx - rr) * q;
   const int hi = lo + (bx < rr ? q + 1 : q);
+  // grid schedule: grid-stride over all pairs; neighbour schedule: own range
+  const bool grid_sched = P.schedule == kScheduleGrid;
+  const int p0 = grid_sched ? bx * blockDim.x + threadIdx.x : lo + threadIdx.x;
+  const int pend = grid_sched ? P.npairs : hi;
+  const int pstep = grid_sched ? G * blockDim.x : blockDim.x;
   const int dep = prob.dep_pairs();
   auto owner = [&](int p) { return p < rr * (q + 1) ? p / (q + 1) : rr + (p - rr * (q + 1)) / max(q, 1); };
   const int c_lo = owner(max(0, lo - dep));
@@ -91,7 +105,7 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(const __grid_constant__
     double2 *__restrict__ ynew = P.y[s_cur ^ 1];
 
     // first stage (block-inline.h:253-272)
-    for (int p = lo + threadIdx.x; p < hi; p += blockDim.x) {
+    for (int p = p0; p < pend; p += pstep) {
       const double2 F = prob.template eval<kExact>(ycur, p);
       const double2 Y = ycur[p];
       for (int l = 1; l < s; ++l) {
@@ -106,15 +120,14 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(const __grid_constant__
       P.dy[p] = make_double2(M::mul(hb[0], F.x), M::mul(hb[0], F.y));
       P.err[p] = make_double2(M::mul(hbh[0], F.x), M::mul(hbh[0], F.y));
     }
-    publish_progress(P.flags, ++progress);
-    if (!(ok = wait_neighbours(P.flags, c_lo, c_hi, progress, st, P.timeout_ns, 1))) break;
+    if (!(ok = stage_sync(P, c_lo, c_hi, ++progress, 1))) break;
 
     // intermediate stages (block-inline.h:276-294)
     for (int i = 1; i < s - 1; ++i) {
       const double2 *__restrict__ wi = P.w[i];
       const double bi = hb[i], bhi = hbh[i];
       const bool nzb = P.nzb[i], nzbh = P.nzbh[i];
-      for (int p = lo + threadIdx.x; p < hi; p += blockDim.x) {
+      for (int p = p0; p < pend; p += pstep) {
         const double2 F = prob.template eval<kExact>(wi, p);
         for (int l = i + 1; l < s; ++l) {
           if (!P.nzA[l * kMaxStages + i]) continue;
@@ -137,8 +150,7 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(const __grid_constant__
           P.err[p] = e;
         }
       }
-      publish_progress(P.flags, ++progress);
-      if (!(ok = wait_neighbours(P.flags, c_lo, c_hi, progress, st, P.timeout_ns, 2))) break;
+      if (!(ok = stage_sync(P, c_lo, c_hi, ++progress, 2))) break;
     }
     if (!ok) break;
 
@@ -149,7 +161,7 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(const __grid_constant__
       const double2 *__restrict__ wl = P.w[i];
       const double bi = hb[i], bhi = hbh[i];
       const bool nzb = P.nzb[i], nzbh = P.nzbh[i];
-      for (int p = lo + threadIdx.x; p < hi; p += blockDim.x) {
+      for (int p = p0; p < pend; p += pstep) {
         const double2 F = prob.template eval<kExact>(wl, p);
         double2 d = P.dy[p];
         double2 e = P.err[p];

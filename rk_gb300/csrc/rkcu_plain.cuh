@@ -28,6 +28,7 @@ struct PlainParams {
   double2 *dy, *err;
   DevState *st;
   unsigned int *flags;                // kMaxPlainGrid progress words (reset by each launch)
+  int schedule;                       // kScheduleGrid or kScheduleNeighbour
   Bruss bruss;
   LvPairs lvp;
   LvBanded lvb;
@@ -35,6 +36,10 @@ struct PlainParams {
 
 // Largest grid the plain kernel uses (the progress words are sized for it).
 constexpr int kMaxPlainGrid = 2048;
+// Stage synchronisation of the plain kernel: a grid barrier after every stage
+// (grid-stride work), or per-CTA ranges with neighbour progress flags.
+constexpr int kScheduleGrid = 1;
+constexpr int kScheduleNeighbour = 2;
 
 // Launches one persistent kernel (cooperative) for up to p.budget steps.
 cudaError_t launch_plain(const PlainParams &p, bool exact, int blocks_per_sm, int num_sms,
