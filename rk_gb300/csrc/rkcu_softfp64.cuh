@@ -1,0 +1,154 @@
+// IEEE-754 binary64 multiply and add, round to nearest even, on 32-bit integer
+// instructions -- host and device.
+//
+// On GB300 the FP64 pipe issues 2 instructions per SM per clock while the SM
+// issues 128 integer instructions per clock, so a double product or sum built
+// from about 30-50 integer instructions costs less issue time than the FP64
+// pipe spends on the hardware instruction, and both can run at once.  These
+// functions give exactly the hardware's result: the fast path covers normal
+// operands with a normal result, everything else (zeros, subnormals,
+// infinities, NaNs, results that overflow or underflow) is handed to the
+// hardware instruction.
+//
+// Method: the 53-bit significands are multiplied exactly as four 32x32->64
+// partial products (106-bit product) or aligned with guard and sticky bits
+// and added in 64-bit registers; the result is rounded to 53 bits, ties to
+// even, and the exponent and significand are assembled with one addition of
+// (exponent - 1) << 52, so that a rounding carry into 2^53 moves the exponent
+// up by itself.
+#pragma once
+
+#include <cstdint>
+#include <cstring>
+
+#ifdef __CUDACC__
+#define SFP_HD __host__ __device__ __forceinline__
+#else
+#define SFP_HD inline
+#endif
+
+namespace rkcu {
+namespace softfp {
+
+SFP_HD uint64_t bits_of(double x) {
+#ifdef __CUDA_ARCH__
+  return static_cast<uint64_t>(__double_as_longlong(x));
+#else
+  uint64_t b;
+  std::memcpy(&b, &x, 8);
+  return b;
+#endif
+}
+
+SFP_HD double double_of(uint64_t b) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double(static_cast<long long>(b));
+#else
+  double x;
+  std::memcpy(&x, &b, 8);
+  return x;
+#endif
+}
+
+SFP_HD int clz64(uint64_t x) {  // x != 0
+#ifdef __CUDA_ARCH__
+  return __clzll(static_cast<long long>(x));
+#else
+  return __builtin_clzll(x);
+#endif
+}
+
+SFP_HD double hw_mul(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __dmul_rn(a, b);
+#else
+  return a * b;
+#endif
+}
+
+SFP_HD double hw_add(double a, double b) {
+#ifdef __CUDA_ARCH__
+  return __dadd_rn(a, b);
+#else
+  return a + b;
+#endif
+}
+
+// a * b rounded to nearest even
+SFP_HD double mul(double a, double b) {
+  const uint64_t ab = bits_of(a), bb = bits_of(b);
+  const uint32_t ahi = static_cast<uint32_t>(ab >> 32), alo = static_cast<uint32_t>(ab);
+  const uint32_t bhi = static_cast<uint32_t>(bb >> 32), blo = static_cast<uint32_t>(bb);
+  const int ea = static_cast<int>((ahi >> 20) & 0x7ff);
+  const int eb = static_cast<int>((bhi >> 20) & 0x7ff);
+  const uint32_t ma = (ahi & 0xfffffu) | 0x100000u;  // high 21 significand bits
+  const uint32_t mb = (bhi & 0xfffffu) | 0x100000u;
+  // 106-bit product  ma:alo * mb:blo = up * 2^64 + mid * 2^32 + low
+  const uint64_t t0 = static_cast<uint64_t>(alo) * blo;
+  const uint64_t t1 = static_cast<uint64_t>(ma) * blo + (t0 >> 32);
+  const uint64_t mm = static_cast<uint64_t>(alo) * mb + t1;  // < 2^55
+  const uint64_t up = static_cast<uint64_t>(ma) * mb + (mm >> 32);  // in [2^40, 2^42)
+  const uint32_t mid = static_cast<uint32_t>(mm);
+  const uint32_t low = static_cast<uint32_t>(t0);
+  const int norm = static_cast<int>(up >> 41);  // product >= 2^105
+  const int e = ea + eb - 1023 + norm;          // biased exponent of the result
+  if (ea == 0 || ea == 0x7ff || eb == 0 || eb == 0x7ff || e < 1 || e > 2046) return hw_mul(a, b);
+  // significand = product >> (52 + norm), 53 bits
+  const int sh = 20 + norm;
+  uint64_t m = (up << (32 - sh)) | (mid >> sh);
+  const uint32_t rbit = (mid >> (sh - 1)) & 1u;
+  const uint32_t sticky = (mid & ((1u << (sh - 1)) - 1u)) | low;
+  m += rbit & ((sticky != 0u) | static_cast<uint32_t>(m & 1u));
+  const uint64_t sign = (ab ^ bb) & 0x8000000000000000ull;
+  return double_of(sign | ((static_cast<uint64_t>(e - 1) << 52) + m));
+}
+
+// a + b rounded to nearest even
+SFP_HD double add(double a, double b) {
+  uint64_t ab = bits_of(a), bb = bits_of(b);
+  // order by magnitude: |a| >= |b|
+  if ((ab & 0x7fffffffffffffffull) < (bb & 0x7fffffffffffffffull)) {
+    const uint64_t t = ab;
+    ab = bb;
+    bb = t;
+  }
+  const int ea = static_cast<int>((ab >> 52) & 0x7ff);
+  const int eb = static_cast<int>((bb >> 52) & 0x7ff);
+  if (ea == 0 || ea == 0x7ff || eb == 0 || eb == 0x7ff) return hw_add(a, b);
+  // significands with the hidden bit at 2^62 (10 guard bits below the 53)
+  const uint64_t ma = ((ab & 0x000fffffffffffffull) | 0x0010000000000000ull) << 10;
+  uint64_t mb = ((bb & 0x000fffffffffffffull) | 0x0010000000000000ull) << 10;
+  const int d = ea - eb;
+  if (d >= 64) {
+    mb = 1;  // only a sticky bit remains
+  } else if (d > 0) {
+    mb = (mb >> d) | static_cast<uint64_t>((mb << (64 - d)) != 0);
+  }
+  const bool subtract = ((ab ^ bb) >> 63) != 0;
+  uint64_t s;
+  int e = ea;
+  if (!subtract) {
+    s = ma + mb;  // < 2^64
+    if (s >> 63) {
+      s = (s >> 1) | (s & 1u);
+      ++e;
+    }
+  } else {
+    s = ma - mb;
+    if (s == 0) return hw_add(a, b);  // exact cancellation: +0 (sign rules) from the hardware
+    const int lz = clz64(s) - 1;        // bring the leading bit to 2^62
+    s <<= lz;
+    e -= lz;
+  }
+  if (e < 1 || e > 2046) return hw_add(a, b);
+  // round 63-bit s to 53 bits: drop 10 bits
+  const uint64_t rbit = (s >> 9) & 1u;
+  const uint64_t sticky = s & 0x1ffu;
+  uint64_t m = s >> 10;
+  m += rbit & ((sticky != 0u) | (m & 1u));
+  const uint64_t sign = ab & 0x8000000000000000ull;
+  return double_of(sign | ((static_cast<uint64_t>(e - 1) << 52) + m));
+}
+
+}  // namespace softfp
+}  // namespace rkcu

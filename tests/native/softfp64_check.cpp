@@ -1,0 +1,61 @@
+// Bit-exactness check of the software binary64 multiply/add (rkcu_softfp64.cuh)
+// against the host's IEEE round-to-nearest arithmetic.  Compiled with
+// -ffp-contract=off.  Usage: softfp64_check <count> <seed>; prints mismatches.
+#include <cinttypes>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+
+#include "rkcu_softfp64.cuh"
+
+using rkcu::softfp::add;
+using rkcu::softfp::bits_of;
+using rkcu::softfp::double_of;
+using rkcu::softfp::mul;
+
+static uint64_t s_state;
+static uint64_t next() {  // splitmix64
+  uint64_t z = (s_state += 0x9e3779b97f4a7c15ull);
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+// a random double of a chosen kind: any bit pattern, values near 1, a given
+// exponent band, or a neighbour of another value (cancellation, near ties)
+static double draw(int kind, double other) {
+  const uint64_t r = next();
+  switch (kind) {
+    case 0: return double_of(r);
+    case 1: return double_of((r & 0x800fffffffffffffull) | (static_cast<uint64_t>(1023 + (int)(r >> 53) % 8 - 4) << 52));
+    case 2: return double_of((r & 0x800fffffffffffffull) | (static_cast<uint64_t>(1 + (r >> 52) % 2046) << 52));
+    case 3: return double_of(bits_of(other) + (static_cast<int64_t>(r % 64) - 32));
+    case 4: return -double_of(bits_of(other) + (r % 5));
+    case 5: return double_of((r & 0x800fffffffffffffull) | (static_cast<uint64_t>((r >> 52) % 2) ? 1ull : 2045ull) << 52);
+    default: return double_of((r & 0xfff0000000000000ull) | (r & 0x7));  // few mantissa bits: ties
+  }
+}
+
+int main(int argc, char **argv) {
+  const long long count = argc > 1 ? atoll(argv[1]) : 10000000;
+  s_state = argc > 2 ? strtoull(argv[2], nullptr, 10) : 1;
+  long long bad_mul = 0, bad_add = 0;
+  for (long long i = 0; i < count; ++i) {
+    const int ka = static_cast<int>(next() % 7);
+    const double a = draw(ka == 3 || ka == 4 ? 1 : ka, 0.0);
+    const double b = draw(static_cast<int>(next() % 7), a);
+    const double pm = a * b, sm = mul(a, b);
+    const double pa = a + b, sa = add(a, b);
+    const bool nan_m = pm != pm && sm != sm, nan_a = pa != pa && sa != sa;
+    if (!nan_m && bits_of(pm) != bits_of(sm)) {
+      if (bad_mul++ < 5)
+        printf("mul %a * %a: hw %a sw %a\n", a, b, pm, sm);
+    }
+    if (!nan_a && bits_of(pa) != bits_of(sa)) {
+      if (bad_add++ < 5)
+        printf("add %a + %a: hw %a sw %a\n", a, b, pa, sa);
+    }
+  }
+  printf("mismatches mul %lld add %lld of %lld\n", bad_mul, bad_add, count);
+  return (bad_mul || bad_add) ? 1 : 0;
+}

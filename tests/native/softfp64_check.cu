@@ -1,0 +1,59 @@
+// Device check of the software binary64 multiply/add (rkcu_softfp64.cuh)
+// against the FP64 pipe's __dmul_rn/__dadd_rn on random and adversarial
+// operands.  Usage: softfp64_check_gpu <count> <seed>; prints mismatches.
+#include <cstdio>
+#include <cstdlib>
+
+#include "rkcu_softfp64.cuh"
+
+using namespace rkcu::softfp;
+
+__device__ __forceinline__ uint64_t mix(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+__device__ double draw(uint64_t r, int kind, double other) {
+  switch (kind) {
+    case 0: return double_of(r);
+    case 1: return double_of((r & 0x800fffffffffffffull) | ((uint64_t)(1023 + (int)(r >> 53) % 8 - 4) << 52));
+    case 2: return double_of((r & 0x800fffffffffffffull) | ((uint64_t)(1 + (r >> 52) % 2046) << 52));
+    case 3: return double_of(bits_of(other) + ((int64_t)(r % 64) - 32));
+    case 4: return -double_of(bits_of(other) + (r % 5));
+    case 5: return double_of((r & 0x800fffffffffffffull) | ((uint64_t)(((r >> 52) % 2) ? 1 : 2045) << 52));
+    default: return double_of((r & 0xfff0000000000000ull) | (r & 0x7));
+  }
+}
+
+__global__ void check(long long count, unsigned long long seed, unsigned long long *bad) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  unsigned long long bm = 0, ba = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += stride) {
+    const uint64_t r0 = mix(seed + 4 * i), r1 = mix(seed + 4 * i + 1), r2 = mix(seed + 4 * i + 2),
+                   r3 = mix(seed + 4 * i + 3);
+    int ka = (int)(r0 % 7);
+    if (ka == 3 || ka == 4) ka = 1;
+    const double a = draw(r1, ka, 0.0);
+    const double b = draw(r3, (int)(r2 % 7), a);
+    const double pm = __dmul_rn(a, b), sm = mul(a, b);
+    const double pa = __dadd_rn(a, b), sa = add(a, b);
+    if (!(pm != pm && sm != sm) && bits_of(pm) != bits_of(sm)) ++bm;
+    if (!(pa != pa && sa != sa) && bits_of(pa) != bits_of(sa)) ++ba;
+  }
+  if (bm) atomicAdd(&bad[0], bm);
+  if (ba) atomicAdd(&bad[1], ba);
+}
+
+int main(int argc, char **argv) {
+  const long long count = argc > 1 ? atoll(argv[1]) : (1ll << 28);
+  const unsigned long long seed = argc > 2 ? strtoull(argv[2], nullptr, 10) : 1;
+  unsigned long long *bad = nullptr, h[2] = {0, 0};
+  if (cudaMalloc(&bad, 2 * sizeof(unsigned long long)) != cudaSuccess) return 2;
+  cudaMemset(bad, 0, 2 * sizeof(unsigned long long));
+  check<<<152 * 8, 256>>>(count, seed, bad);
+  if (cudaMemcpy(h, bad, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) return 2;
+  printf("mismatches mul %llu add %llu of %lld\n", h[0], h[1], count);
+  cudaFree(bad);
+  return (h[0] || h[1]) ? 1 : 0;
+}
