@@ -63,7 +63,7 @@ def fp64_ops_per_comp(method, precision):
     nz_a = int(np.count_nonzero(np.tril(m["A"], -1)))
     nz_b = int(np.count_nonzero(m["b"]))
     nz_bh = int(np.count_nonzero(m["b"] - m["b_hat"]))
-    if precision == "exact":
+    if precision.startswith("exact"):
         return 9.5 * s + 2 * nz_a + (2 * nz_b - 1) + (2 * nz_bh - 1) + 1.5
     return 7.5 * s + nz_a + nz_b + nz_bh + 1.5
 
@@ -518,7 +518,7 @@ def main():
     ap.add_argument("--method", default="DOPRI54")
     ap.add_argument("--grid", type=int, default=GRID_N,
                     help="grid size N (2000 is the benchmark; smaller only for profiling)")
-    ap.add_argument("--precision", default="exact", choices=["exact", "fma", "mixed"],
+    ap.add_argument("--precision", default="exact", choices=["exact", "exact-hwmul", "fma", "mixed"],
                     help="exact (default): bit-identical to the reference; fma: fewer FP64 "
                          "instructions; mixed: FP32 stage vectors (the N=4000 configuration)")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -46,6 +46,9 @@ extern "C" {
                                 differs from the reference in the last bits, which can
                                 change accept/reject decisions of stiff problems */
 #define RKCU_MIXED       2   /* FP32 stage vectors, FP64 state, update and error norm */
+#define RKCU_FP64_EXACT_HWMUL 3 /* RKCU_FP64_EXACT with every product on the FP64 pipe (the
+                                default exact mode computes products on the integer pipe,
+                                bit for bit the same; this one exists to compare them) */
 
 /* ---- solver variants (src/impl/seq/D.c, src/impl/seq/PipeDls.c) ------- */
 #define RKCU_VARIANT_D           0   /* stage vectors w_1..w_{s-1}, dy, err in HBM */

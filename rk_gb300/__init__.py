@@ -36,6 +36,7 @@ PROBLEM_LV_BANDED = 2
 FP64_EXACT = 0
 FP64_FMA = 1
 MIXED = 2
+FP64_EXACT_HWMUL = 3
 
 VARIANT_D = 0
 VARIANT_LOWSTORAGE = 1
@@ -273,7 +274,8 @@ def step_sizes(h, err, tol, ord, device=False):
     return out, flags.astype(bool)
 
 
-_PREC = {"exact": FP64_EXACT, "fp64": FP64_EXACT, "fma": FP64_FMA, "mixed": MIXED}
+_PREC = {"exact": FP64_EXACT, "fp64": FP64_EXACT, "fma": FP64_FMA, "mixed": MIXED,
+         "exact-hwmul": FP64_EXACT_HWMUL}
 
 
 class Solver:

@@ -150,7 +150,8 @@ int rkcu_create(rkcu_solver **out, const rkcu_problem *prob, const rkcu_options 
     o = *opt;
   else
     rkcu_options_default(&o);
-  if (o.precision != RKCU_FP64_EXACT && o.precision != RKCU_FP64_FMA && o.precision != RKCU_MIXED)
+  if (o.precision != RKCU_FP64_EXACT && o.precision != RKCU_FP64_FMA && o.precision != RKCU_MIXED &&
+      o.precision != RKCU_FP64_EXACT_HWMUL)
     return RKCU_ERR_INVALID;
   if (o.precision == RKCU_MIXED && prob->problem != RKCU_PROBLEM_BRUSS2D_MIX) return RKCU_ERR_INVALID;
   if (o.variant != RKCU_VARIANT_D && o.variant != RKCU_VARIANT_LOWSTORAGE) return RKCU_ERR_INVALID;
@@ -376,7 +377,7 @@ int rkcu_advance(rkcu_solver *s, int max_steps) {
     q.bruss.N = N;
     q.bruss.coef = bruss_coef(&s->prob);
     int grid = 0;
-    cudaError_t e = rkcu::launch_lowstorage(q, s->opt.precision == RKCU_FP64_EXACT, s->num_sms,
+    cudaError_t e = rkcu::launch_lowstorage(q, s->opt.precision != RKCU_FP64_FMA, s->num_sms,
                                             s->stream, &grid);
     if (e != cudaSuccess) return cuda_fail(e, "low-storage kernel launch");
     s->last_grid = grid;
@@ -465,8 +466,10 @@ int rkcu_advance(rkcu_solver *s, int max_steps) {
   p.lvb.a = s->lv_a;
   p.extra_arrivals = s->extra_arrivals;
   int grid = 0;
-  cudaError_t e = rkcu::launch_plain(p, s->opt.precision == RKCU_FP64_EXACT, 0, s->num_sms,
-                                     s->stream, &grid);
+  const int mode = s->opt.precision == RKCU_FP64_EXACT        ? rkcu::kArithExactSoftMul
+                   : s->opt.precision == RKCU_FP64_EXACT_HWMUL ? rkcu::kArithExact
+                                                               : rkcu::kArithFused;
+  cudaError_t e = rkcu::launch_plain(p, mode, 0, s->num_sms, s->stream, &grid);
   if (e != cudaSuccess) return cuda_fail(e, "plain kernel launch");
   s->last_grid = grid;
   ++s->launches;

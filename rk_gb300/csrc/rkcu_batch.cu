@@ -18,7 +18,7 @@
 
 namespace rkcu {
 
-template <bool kExact>
+template <int kExact>
 __device__ __forceinline__ double2 batch_rhs(const InstDesc &d, const double2 *w, int p) {
   switch (d.kind) {
     case RKCU_PROBLEM_BRUSS2D_MIX: {
@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(kT) batch_rebuild_kernel(const __grid_constant
   rebuild_chunks<kT>(P);
 }
 
-template <bool kExact, int kT>
+template <int kExact, int kT>
 __global__ void __launch_bounds__(kT) batch_kernel(const __grid_constant__ BatchParams P) {
   using M = Arith<kExact>;
   __shared__ double s_wmax[kT / 32];
@@ -229,7 +229,7 @@ cudaError_t launch_batch_rebuild(const BatchParams &p, cudaStream_t stream) {
   return cudaGetLastError();
 }
 
-template <bool kExact, int kT>
+template <int kExact, int kT>
 static int grid_of(int blocks_per_sm, int num_sms) {
   int occ = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel<kExact, kT>, kT, 0) !=
@@ -242,13 +242,16 @@ static int grid_of(int blocks_per_sm, int num_sms) {
 
 int batch_grid(bool exact, int threads, int blocks_per_sm, int num_sms) {
   if (threads == 128)
-    return exact ? grid_of<true, 128>(blocks_per_sm, num_sms) : grid_of<false, 128>(blocks_per_sm, num_sms);
+    return exact ? grid_of<kArithExact, 128>(blocks_per_sm, num_sms)
+                 : grid_of<kArithFused, 128>(blocks_per_sm, num_sms);
   if (threads == 512)
-    return exact ? grid_of<true, 512>(blocks_per_sm, num_sms) : grid_of<false, 512>(blocks_per_sm, num_sms);
-  return exact ? grid_of<true, 256>(blocks_per_sm, num_sms) : grid_of<false, 256>(blocks_per_sm, num_sms);
+    return exact ? grid_of<kArithExact, 512>(blocks_per_sm, num_sms)
+                 : grid_of<kArithFused, 512>(blocks_per_sm, num_sms);
+  return exact ? grid_of<kArithExact, 256>(blocks_per_sm, num_sms)
+               : grid_of<kArithFused, 256>(blocks_per_sm, num_sms);
 }
 
-template <bool kExact, int kT>
+template <int kExact, int kT>
 static cudaError_t launch_t(const BatchParams &p, int grid, cudaStream_t stream) {
   BatchParams q = p;
   q.nblocks = grid;
@@ -271,10 +274,10 @@ cudaError_t launch_batch(const BatchParams &p, bool exact, int threads, int bloc
   if (grid <= 0) return cudaErrorInvalidConfiguration;
   *grid_out = grid;
   if (threads == 128)
-    return exact ? launch_t<true, 128>(p, grid, stream) : launch_t<false, 128>(p, grid, stream);
+    return exact ? launch_t<kArithExact, 128>(p, grid, stream) : launch_t<kArithFused, 128>(p, grid, stream);
   if (threads == 512)
-    return exact ? launch_t<true, 512>(p, grid, stream) : launch_t<false, 512>(p, grid, stream);
-  return exact ? launch_t<true, 256>(p, grid, stream) : launch_t<false, 256>(p, grid, stream);
+    return exact ? launch_t<kArithExact, 512>(p, grid, stream) : launch_t<kArithFused, 512>(p, grid, stream);
+  return exact ? launch_t<kArithExact, 256>(p, grid, stream) : launch_t<kArithFused, 256>(p, grid, stream);
 }
 
 }  // namespace rkcu

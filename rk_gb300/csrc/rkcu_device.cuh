@@ -6,26 +6,36 @@
 #include <cuda_runtime.h>
 
 #include "rkcu_pow.cuh"
+#include "rkcu_softfp64.cuh"
 
 namespace rkcu {
 
 constexpr int kMaxStages = 13;   // DOPRI87 (src/methods.c:476) is the largest tableau
 
 // ---------------------------------------------------------------------------
-// Arithmetic policies.
+// Arithmetic policies (template argument kExact of the evaluators and kernels).
 //
-// Exact: every product and sum is rounded once, in the order the reference's C
-// expressions imply, with explicit round-to-nearest intrinsics so that nvcc
-// cannot contract them into FMAs.  The two FMAs it does use, fma(-4,y,s) and
-// fma(2,y,s), are exact rewrites: 4y and 2y are exact in binary floating point,
-// so fma(-4,y,s) == s - 4.0*y rounded once, as in the reference.
-// Fused: contracts a*b+c into one FMA (fewer FP64 instructions).
+// kArithExact (1): every product and sum is rounded once, in the order the
+// reference's C expressions imply, with explicit round-to-nearest intrinsics
+// so that nvcc cannot contract them into FMAs.  The two FMAs it does use,
+// fma(-4,y,s) and fma(2,y,s), are exact rewrites: 4y and 2y are exact in
+// binary floating point, so fma(-4,y,s) == s - 4.0*y rounded once, as in the
+// reference.
+// kArithExactSoftMul (2): the same results bit for bit, with the products
+// computed on the integer pipe (rkcu_softfp64.cuh) while the sums stay on the
+// FP64 pipe -- on this part the FP64 pipe is the bottleneck and the integer
+// issue slots are idle.
+// kArithFused (0): contracts a*b+c into one FMA (fewer FP64 instructions).
 // ---------------------------------------------------------------------------
-template <bool kExact>
+constexpr int kArithFused = 0;
+constexpr int kArithExact = 1;
+constexpr int kArithExactSoftMul = 2;
+
+template <int kMode>
 struct Arith;
 
 template <>
-struct Arith<true> {
+struct Arith<kArithExact> {
   static __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
   static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
   static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
@@ -40,7 +50,20 @@ struct Arith<true> {
 };
 
 template <>
-struct Arith<false> {
+struct Arith<kArithExactSoftMul> {
+  static __device__ __forceinline__ double mul(double a, double b) { return softfp::mul(a, b); }
+  static __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+  static __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+  static __device__ __forceinline__ double mac(double acc, double a, double b) {
+    return __dadd_rn(acc, softfp::mul(a, b));
+  }
+  static __device__ __forceinline__ double msub(double a, double b, double c) {
+    return __dsub_rn(softfp::mul(a, b), c);
+  }
+};
+
+template <>
+struct Arith<kArithFused> {
   static __device__ __forceinline__ double mul(double a, double b) { return a * b; }
   static __device__ __forceinline__ double add(double a, double b) { return a + b; }
   static __device__ __forceinline__ double sub(double a, double b) { return a - b; }
@@ -68,7 +91,7 @@ struct Bruss {
   // pairs on either side a point's stencil reaches: one grid row (ode_acc_dist = 2N components)
   __device__ __forceinline__ int dep_pairs() const { return N; }
 
-  template <bool kExact>
+  template <int kExact>
   __device__ __forceinline__ double2 eval(const double2 *__restrict__ w, int p) const {
     const int k = p / N;
     const int j = p - k * N;
@@ -79,7 +102,7 @@ struct Bruss {
   // Same, given the grid rows above (`up`: row k-1, or row k+1 on the first row),
   // at (`cr`: row k) and below (`dn`: row k+1, or row k-1 on the last row) of the
   // point, each indexed by column; lets stage vectors live in ring buffers.
-  template <bool kExact>
+  template <int kExact>
   __device__ __forceinline__ double2 eval_rows(const double2 *__restrict__ upr,
                                                const double2 *__restrict__ cr,
                                                const double2 *__restrict__ dnr, int j) const {
@@ -118,7 +141,7 @@ struct Bruss {
 //   prey  f0 = c0*y0 - d0*y0*y1,  predator f1 = d1*y0*y1 - c1*y1
 struct LvPairs {
   __device__ __forceinline__ int dep_pairs() const { return 0; }
-  template <bool kExact>
+  template <int kExact>
   __device__ __forceinline__ double2 eval(const double2 *__restrict__ w, int p) const {
     using M = Arith<kExact>;
     const double2 c = w[p];
@@ -136,7 +159,7 @@ struct LvBanded {
   const double *__restrict__ a;  // a[n_pad][5]
   __device__ __forceinline__ int dep_pairs() const { return 1; }
 
-  template <bool kExact>
+  template <int kExact>
   __device__ __forceinline__ double comp(const double *__restrict__ y, int i) const {
     using M = Arith<kExact>;
     double acc = r[i];
@@ -147,7 +170,7 @@ struct LvBanded {
     }
     return M::mul(y[i], acc);
   }
-  template <bool kExact>
+  template <int kExact>
   __device__ __forceinline__ double2 eval(const double2 *__restrict__ w, int p) const {
     const double *y = reinterpret_cast<const double *>(w);
     const int i = 2 * p;

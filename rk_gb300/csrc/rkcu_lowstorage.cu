@@ -22,7 +22,7 @@ namespace rkcu {
 
 constexpr int kLsThreads = 256;
 
-template <bool kExact>
+template <int kExact>
 __global__ void __launch_bounds__(kLsThreads) ls_kernel(const __grid_constant__ LsParams P) {
   using M = Arith<kExact>;
   __shared__ double hA[kMaxStages * kMaxStages];
@@ -239,7 +239,7 @@ __global__ void __launch_bounds__(kLsThreads) ls_kernel(const __grid_constant__ 
   }
 }
 
-template <bool kExact>
+template <int kExact>
 static cudaError_t launch_t(const LsParams &p, int num_sms, cudaStream_t stream, int *grid_out) {
   int occ = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, ls_kernel<kExact>, kLsThreads, 0);
@@ -256,8 +256,8 @@ static cudaError_t launch_t(const LsParams &p, int num_sms, cudaStream_t stream,
 
 cudaError_t launch_lowstorage(const LsParams &p, bool exact, int num_sms, cudaStream_t stream,
                               int *grid_out) {
-  return exact ? launch_t<true>(p, num_sms, stream, grid_out)
-               : launch_t<false>(p, num_sms, stream, grid_out);
+  return exact ? launch_t<kArithExact>(p, num_sms, stream, grid_out)
+               : launch_t<kArithFused>(p, num_sms, stream, grid_out);
 }
 
 size_t lowstorage_ring_pairs(int s, int R, int N) {

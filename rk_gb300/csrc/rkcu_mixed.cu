@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(kMixThreads) mixed_kernel(const __grid_constan
     {
       const double hbs = s_hbsum;
       for (int p = gtid; p < P.npairs; p += gstride) {
-        const double2 F = br.eval<false>(ycur, p);
+        const double2 F = br.eval<kArithFused>(ycur, p);
         const double2 Y = ycur[p];
         ynew[p] = make_double2(fma(hbs, F.x, Y.x), fma(hbs, F.y, Y.y));
         P.f0[p] = make_float2(__double2float_rn(F.x), __double2float_rn(F.y));

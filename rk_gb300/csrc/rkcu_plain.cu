@@ -42,7 +42,7 @@ __device__ __forceinline__ bool stage_sync(const PlainParams &P, int c_lo, int c
   return wait_neighbours(P.flags, c_lo, c_hi, progress, P.st, P.timeout_ns, site);
 }
 
-template <class Prob, bool kExact>
+template <class Prob, int kExact>
 __global__ void __launch_bounds__(kThreads) plain_kernel(const __grid_constant__ PlainParams P) {
   using M = Arith<kExact>;
   __shared__ double hA[kMaxStages * kMaxStages];
@@ -255,10 +255,10 @@ __global__ void __launch_bounds__(kThreads) eval_rhs_kernel(Prob prob, int npair
                                                             const double2 *__restrict__ y,
                                                             double2 *__restrict__ f) {
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npairs; p += gridDim.x * blockDim.x)
-    f[p] = prob.template eval<true>(y, p);
+    f[p] = prob.template eval<kArithExact>(y, p);
 }
 
-template <class Prob, bool kExact>
+template <class Prob, int kExact>
 static cudaError_t launch_one(const PlainParams &p, int blocks_per_sm, int num_sms,
                               cudaStream_t stream, int *grid_out) {
   auto kern = plain_kernel<Prob, kExact>;
@@ -281,18 +281,26 @@ static cudaError_t launch_one(const PlainParams &p, int blocks_per_sm, int num_s
                                      stream);
 }
 
-cudaError_t launch_plain(const PlainParams &p, bool exact, int blocks_per_sm, int num_sms,
+template <class Prob>
+static cudaError_t launch_mode(const PlainParams &p, int mode, int blocks_per_sm, int num_sms,
+                               cudaStream_t stream, int *grid_out) {
+  switch (mode) {
+    case kArithExact: return launch_one<Prob, kArithExact>(p, blocks_per_sm, num_sms, stream, grid_out);
+    case kArithExactSoftMul:
+      return launch_one<Prob, kArithExactSoftMul>(p, blocks_per_sm, num_sms, stream, grid_out);
+    default: return launch_one<Prob, kArithFused>(p, blocks_per_sm, num_sms, stream, grid_out);
+  }
+}
+
+cudaError_t launch_plain(const PlainParams &p, int mode, int blocks_per_sm, int num_sms,
                          cudaStream_t stream, int *grid_out) {
   switch (p.problem) {
     case RKCU_PROBLEM_BRUSS2D_MIX:
-      return exact ? launch_one<Bruss, true>(p, blocks_per_sm, num_sms, stream, grid_out)
-                   : launch_one<Bruss, false>(p, blocks_per_sm, num_sms, stream, grid_out);
+      return launch_mode<Bruss>(p, mode, blocks_per_sm, num_sms, stream, grid_out);
     case RKCU_PROBLEM_LV_PAIRS:
-      return exact ? launch_one<LvPairs, true>(p, blocks_per_sm, num_sms, stream, grid_out)
-                   : launch_one<LvPairs, false>(p, blocks_per_sm, num_sms, stream, grid_out);
+      return launch_mode<LvPairs>(p, mode, blocks_per_sm, num_sms, stream, grid_out);
     case RKCU_PROBLEM_LV_BANDED:
-      return exact ? launch_one<LvBanded, true>(p, blocks_per_sm, num_sms, stream, grid_out)
-                   : launch_one<LvBanded, false>(p, blocks_per_sm, num_sms, stream, grid_out);
+      return launch_mode<LvBanded>(p, mode, blocks_per_sm, num_sms, stream, grid_out);
     default:
       return cudaErrorInvalidValue;
   }

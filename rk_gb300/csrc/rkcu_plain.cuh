@@ -42,7 +42,8 @@ constexpr int kScheduleGrid = 1;
 constexpr int kScheduleNeighbour = 2;
 
 // Launches one persistent kernel (cooperative) for up to p.budget steps.
-cudaError_t launch_plain(const PlainParams &p, bool exact, int blocks_per_sm, int num_sms,
+// mode: kArithFused, kArithExact or kArithExactSoftMul
+cudaError_t launch_plain(const PlainParams &p, int mode, int blocks_per_sm, int num_sms,
                          cudaStream_t stream, int *grid_out);
 
 // Device RHS over all pairs of y (exact arithmetic), for ode_eval_rng.

@@ -180,3 +180,15 @@ def test_bad_calls_are_rejected():
         with pytest.raises(rk.RkcuError) as ei:
             s.advance(3)                          # nothing begun
         assert ei.value.status == rk.ERR_STATE
+
+
+@pytest.mark.parametrize("name", ["bruss_n250_dopri54_tol1e-6", "bruss_n64_dopri87_tol1e-7",
+                                  "lv_pairs_1000_dopri54"])
+def test_products_on_integer_pipe_equal_fp64_pipe(name):
+    """The default exact mode computes products on the integer pipe; with every
+    product on the FP64 pipe the results are the same bit for bit."""
+    rec = load_golden(name)
+    a, sa = _solve(rec, "exact")
+    b, sb = _solve(rec, "exact-hwmul")
+    np.testing.assert_array_equal(a, b)
+    assert (sa["steps_acc"], sa["steps_rej"]) == (sb["steps_acc"], sb["steps_rej"])
