@@ -270,13 +270,17 @@ struct ErrMax {
     // a subnormal or zero divisor would make the estimate too low: exact path
     const bool special = ae >= kInf || an > kInf || ao > kInf || d < kMinNormal;
     const int key = static_cast<int>(ae >> 32) - static_cast<int>(d >> 32);
-    if (special || key > best_key - kMargin) {
-      const double div = fmax(fabs(yn), fabs(yo));
-      const double r = div == 0.0 ? 1.7E308 : fabs(e) / div;
-      if (r > best) {  // false for NaN, as fmax would ignore it
-        best = r;
-        best_key = static_cast<int>(__double_as_longlong(r) >> 32) - 0x3ff00000;
-      }
+    if (special || key > best_key - kMargin) update(e, yn, yo);
+  }
+
+  // the exact path, kept out of line so that the division is not if-converted
+  // (run for every lane) by the compiler
+  __device__ __noinline__ void update(double e, double yn, double yo) {
+    const double div = fmax(fabs(yn), fabs(yo));
+    const double r = div == 0.0 ? 1.7E308 : fabs(e) / div;
+    if (r > best) {  // false for NaN, as fmax would ignore it
+      best = r;
+      best_key = static_cast<int>(__double_as_longlong(r) >> 32) - 0x3ff00000;
     }
   }
 };

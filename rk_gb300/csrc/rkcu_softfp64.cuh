@@ -58,7 +58,14 @@ SFP_HD int clz64(uint64_t x) {  // x != 0
 #endif
 }
 
-SFP_HD double hw_mul(double a, double b) {
+// The rare paths are real calls, not inlined: inlined, the compiler would
+// if-convert them and run the FP64 instruction for every lane, which would
+// defeat the purpose of moving the product off the FP64 pipe.
+#ifdef __CUDACC__
+static __host__ __device__ __noinline__ double hw_mul(double a, double b) {
+#else
+inline double hw_mul(double a, double b) {
+#endif
 #ifdef __CUDA_ARCH__
   return __dmul_rn(a, b);
 #else
@@ -66,7 +73,11 @@ SFP_HD double hw_mul(double a, double b) {
 #endif
 }
 
-SFP_HD double hw_add(double a, double b) {
+#ifdef __CUDACC__
+static __host__ __device__ __noinline__ double hw_add(double a, double b) {
+#else
+inline double hw_add(double a, double b) {
+#endif
 #ifdef __CUDA_ARCH__
   return __dadd_rn(a, b);
 #else
