@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(kT) batch_kernel(const __grid_constant__ Batch
         double2 *__restrict__ dy = vec + static_cast<size_t>(s + 1) * np;
         double2 *__restrict__ er = vec + static_cast<size_t>(s + 2) * np;
         const int pend = min(ch.y + P.chunk_pairs, d.npairs);
-        double emax = 0.0;
+        ErrMax em;
         if (i == 0) {
           for (int p = ch.y + threadIdx.x; p < pend; p += kT) {
             const double2 F = batch_rhs<kExact>(d, ycur, p);
@@ -141,16 +141,13 @@ __global__ void __launch_bounds__(kT) batch_kernel(const __grid_constant__ Batch
               const double2 Y = ycur[p];
               const double2 yn = make_double2(M::add(Y.x, dd.x), M::add(Y.y, dd.y));
               ynew[p] = yn;
-              double div = fmax(fabs(yn.x), fabs(Y.x));
-              emax = fmax(emax, div == 0.0 ? 1.7E308 : fabs(e.x) / div);
-              if (2 * p + 1 < d.n) {
-                div = fmax(fabs(yn.y), fabs(Y.y));
-                emax = fmax(emax, div == 0.0 ? 1.7E308 : fabs(e.y) / div);
-              }
+              em.add(e.x, yn.x, Y.x);
+              if (2 * p + 1 < d.n) em.add(e.y, yn.y, Y.y);
             }
           }
         }
         if (last) {
+          double emax = em.best;
 #pragma unroll
           for (int off = 16; off > 0; off >>= 1)
             emax = fmax(emax, __shfl_xor_sync(0xffffffffu, emax, off));
@@ -242,12 +239,12 @@ static int grid_of(int blocks_per_sm, int num_sms) {
 
 int batch_grid(bool exact, int threads, int blocks_per_sm, int num_sms) {
   if (threads == 128)
-    return exact ? grid_of<kArithExact, 128>(blocks_per_sm, num_sms)
+    return exact ? grid_of<kArithExactSoftMul, 128>(blocks_per_sm, num_sms)
                  : grid_of<kArithFused, 128>(blocks_per_sm, num_sms);
   if (threads == 512)
-    return exact ? grid_of<kArithExact, 512>(blocks_per_sm, num_sms)
+    return exact ? grid_of<kArithExactSoftMul, 512>(blocks_per_sm, num_sms)
                  : grid_of<kArithFused, 512>(blocks_per_sm, num_sms);
-  return exact ? grid_of<kArithExact, 256>(blocks_per_sm, num_sms)
+  return exact ? grid_of<kArithExactSoftMul, 256>(blocks_per_sm, num_sms)
                : grid_of<kArithFused, 256>(blocks_per_sm, num_sms);
 }
 
@@ -274,10 +271,10 @@ cudaError_t launch_batch(const BatchParams &p, bool exact, int threads, int bloc
   if (grid <= 0) return cudaErrorInvalidConfiguration;
   *grid_out = grid;
   if (threads == 128)
-    return exact ? launch_t<kArithExact, 128>(p, grid, stream) : launch_t<kArithFused, 128>(p, grid, stream);
+    return exact ? launch_t<kArithExactSoftMul, 128>(p, grid, stream) : launch_t<kArithFused, 128>(p, grid, stream);
   if (threads == 512)
-    return exact ? launch_t<kArithExact, 512>(p, grid, stream) : launch_t<kArithFused, 512>(p, grid, stream);
-  return exact ? launch_t<kArithExact, 256>(p, grid, stream) : launch_t<kArithFused, 256>(p, grid, stream);
+    return exact ? launch_t<kArithExactSoftMul, 512>(p, grid, stream) : launch_t<kArithFused, 512>(p, grid, stream);
+  return exact ? launch_t<kArithExactSoftMul, 256>(p, grid, stream) : launch_t<kArithFused, 256>(p, grid, stream);
 }
 
 }  // namespace rkcu

@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(kLsThreads) ls_kernel(const __grid_constant__ 
     __syncthreads();
     const double2 *__restrict__ ycur = P.y[s_cur];
     double2 *__restrict__ ynew = P.y[s_cur ^ 1];
-    double emax = 0.0;
+    ErrMax em;
 
     const int ntau = nb + 2 * (s - 1);
     for (int tau = 0; tau < ntau && ok; ++tau) {
@@ -159,10 +159,8 @@ __global__ void __launch_bounds__(kLsThreads) ls_kernel(const __grid_constant__ 
             const double2 Y = ycur[g];
             const double2 yn = make_double2(M::add(Y.x, dd.x), M::add(Y.y, dd.y));
             ynew[g] = yn;
-            double dv = fmax(fabs(yn.x), fabs(Y.x));
-            emax = fmax(emax, dv == 0.0 ? 1.7E308 : fabs(e.x) / dv);
-            dv = fmax(fabs(yn.y), fabs(Y.y));
-            emax = fmax(emax, dv == 0.0 ? 1.7E308 : fabs(e.y) / dv);
+            em.add(e.x, yn.x, Y.x);
+            em.add(e.y, yn.y, Y.y);
           }
         }
       }
@@ -170,6 +168,7 @@ __global__ void __launch_bounds__(kLsThreads) ls_kernel(const __grid_constant__ 
     }
     if (!ok) break;
 
+    double emax = em.best;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) emax = fmax(emax, __shfl_xor_sync(0xffffffffu, emax, off));
     if (lane == 0) s_wmax[warp] = emax;
@@ -256,7 +255,7 @@ static cudaError_t launch_t(const LsParams &p, int num_sms, cudaStream_t stream,
 
 cudaError_t launch_lowstorage(const LsParams &p, bool exact, int num_sms, cudaStream_t stream,
                               int *grid_out) {
-  return exact ? launch_t<kArithExact>(p, num_sms, stream, grid_out)
+  return exact ? launch_t<kArithExactSoftMul>(p, num_sms, stream, grid_out)
                : launch_t<kArithFused>(p, num_sms, stream, grid_out);
 }
 

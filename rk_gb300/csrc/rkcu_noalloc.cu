@@ -159,7 +159,7 @@ extern "C" int rkcu_solve_noalloc(const rkcu_problem *prob, const char *method, 
     if (hs.done) break;
     p.budget = 1 << 20;
     int grid = 0;
-    if ((e = rkcu::launch_plain(p, precision == RKCU_FP64_EXACT ? rkcu::kArithExact : rkcu::kArithFused, 0,
+    if ((e = rkcu::launch_plain(p, precision == RKCU_FP64_EXACT ? rkcu::kArithExactSoftMul : rkcu::kArithFused, 0,
                                    num_sms, st, &grid)) !=
         cudaSuccess)
       return fail_cuda(e, "step-loop launch");
