@@ -304,6 +304,7 @@ typedef struct
   double *y, *w[ORK_MAX_STAGES], *dy, *err;
   double *slot;                 /* per-thread err_max, padded */
   pthread_barrier_t bar;
+  int rows;                     /* > 0: pipelined schedule with blocks of this many rows */
   ork_stats *stats;
   double *h_trace;
   int trace_cap;
@@ -318,6 +319,58 @@ static inline double eval_at(const solve_ctx *x, int j, const double *arg)
   return ork_eval_comp(x->p, j, arg);
 }
 
+/*
+ * BRUSS2D-MIX components [c0, c1) of f(y) into F[0 .. c1-c0): bruss_comp's
+ * expressions with the grid position stepped along instead of divided out.
+ */
+static void bruss_range(int N, double coef, int c0, int c1, const double *y, double *F)
+{
+  const int N2 = N + N;
+  int k = c0 / N2, r = c0 - k * N2, i;
+  for (i = c0; i < c1; i++)
+  {
+    const int j = r >> 1, isv = r & 1;
+    const double u = y[i - isv], v = y[i - isv + 1];
+    const double up = (k == 0) ? y[i + N2] : y[i - N2];
+    const double dn = (k == N - 1) ? y[i - N2] : y[i + N2];
+    const double vert = up + dn;
+    double lap, react;
+    if (j == 0)
+      lap = vert + 2.0 * y[i + 2];
+    else if (j == N - 1)
+      lap = vert + 2.0 * y[i - 2];
+    else
+      lap = vert + y[i - 2] + y[i + 2];
+    lap = lap - 4.0 * y[i];
+    if (isv)
+      react = 3.4 * u - u * u * v;
+    else
+      react = 1.0 + u * u * v - 4.4 * u;
+    F[i - c0] = react + coef * lap;
+    if (++r == N2)
+    {
+      r = 0;
+      k++;
+    }
+  }
+}
+
+/* f(arg) on components [c0, c1) into F[0 .. c1-c0) */
+static void eval_range(const solve_ctx *x, int c0, int c1, const double *arg, double *F)
+{
+  int j;
+  if (x->p->kind == ORK_BRUSS2D_MIX)
+  {
+    bruss_range(x->p->grid_n, x->coef, c0, c1, arg, F);
+    return;
+  }
+  for (j = c0; j < c1; j++)
+    F[j - c0] = ork_eval_comp(x->p, j, arg);
+}
+
+/* components per chunk of the stage loops (F of one chunk stays in L1) */
+#define ORK_CHUNK 512
+
 /* tools.h:221-233 */
 static double h_new(double h, double err, double tol, int ord)
 {
@@ -331,6 +384,116 @@ double ork_h_new(double h, double err, double tol, int ord)
   return h_new(h, err, tol, ord);
 }
 
+/* block-inline.h:253-272, components [c0, c1) */
+static void stage_first(solve_ctx *x, double hA[][ORK_MAX_STAGES], const double *hb,
+                        const double *hbh, int c0, int c1)
+{
+  const int s = x->s;
+  double *y = x->y, *dy = x->dy, *err = x->err;
+  double F[ORK_CHUNK];
+  int a, j, l;
+  for (a = c0; a < c1; a += ORK_CHUNK)
+  {
+    const int e = c1 - a < ORK_CHUNK ? c1 : a + ORK_CHUNK;
+    eval_range(x, a, e, y, F);
+    for (l = 1; l < s; l++)
+    {
+      const double al = hA[l][0];
+      double *wl = x->w[l];
+      for (j = a; j < e; j++)
+        wl[j] = y[j] + al * F[j - a];
+    }
+    for (j = a; j < e; j++)
+    {
+      dy[j] = hb[0] * F[j - a];
+      err[j] = hbh[0] * F[j - a];
+    }
+  }
+}
+
+/* block-inline.h:276-294 */
+static void stage_mid(solve_ctx *x, int i, double hA[][ORK_MAX_STAGES], const double *hb,
+                      const double *hbh, int c0, int c1)
+{
+  const int s = x->s;
+  const double *wi = x->w[i];
+  double *dy = x->dy, *err = x->err;
+  double F[ORK_CHUNK];
+  int a, j, l;
+  for (a = c0; a < c1; a += ORK_CHUNK)
+  {
+    const int e = c1 - a < ORK_CHUNK ? c1 : a + ORK_CHUNK;
+    eval_range(x, a, e, wi, F);
+    for (l = i + 1; l < s; l++)
+    {
+      const double al = hA[l][i];
+      double *wl = x->w[l];
+      for (j = a; j < e; j++)
+        wl[j] += al * F[j - a];
+    }
+    for (j = a; j < e; j++)
+    {
+      dy[j] += hb[i] * F[j - a];
+      err[j] += hbh[i] * F[j - a];
+    }
+  }
+}
+
+/* block-inline.h:298-320, tools.h:280-288 */
+static void stage_last(solve_ctx *x, const double *hb, const double *hbh, int c0, int c1,
+                       double *emax)
+{
+  const int i = x->s - 1;
+  const double *wl = x->w[i];
+  double *y = x->y, *dy = x->dy, *err = x->err;
+  double F[ORK_CHUNK];
+  int a, j;
+  for (a = c0; a < c1; a += ORK_CHUNK)
+  {
+    const int e = c1 - a < ORK_CHUNK ? c1 : a + ORK_CHUNK;
+    eval_range(x, a, e, wl, F);
+    for (j = a; j < e; j++)
+    {
+      double yold, div;
+      dy[j] += hb[i] * F[j - a];
+      err[j] += hbh[i] * F[j - a];
+      yold = y[j];
+      y[j] += dy[j];
+      dy[j] = yold;
+      div = fmax(fabs(y[j]), fabs(yold));
+      if (div == 0.0)
+        *emax = 1.7E308;
+      else
+        *emax = fmax(*emax, fabs(err[j]) / div);
+    }
+  }
+}
+
+/* Stage i over components [c0, c1) */
+static void stage_range(solve_ctx *x, int i, double hA[][ORK_MAX_STAGES], const double *hb,
+                        const double *hbh, int c0, int c1, double *emax)
+{
+  if (i == 0)
+    stage_first(x, hA, hb, hbh, c0, c1);
+  else if (i < x->s - 1)
+    stage_mid(x, i, hA, hb, hbh, c0, c1);
+  else
+    stage_last(x, hb, hbh, c0, c1, emax);
+}
+
+/*
+ * The step of one thread.  Schedule D (x->rows == 0): stage by stage over the
+ * thread's block of components, a barrier between stages (pthreads/D.c).
+ * Pipelined schedule (x->rows != 0, BRUSS2D-MIX; the idea of the reference's
+ * PipeD variants, seq/PipeD.c:62-124): every thread owns a slab of grid rows
+ * and sweeps it diagonally, stage i on row tau - i, so the stage vectors of a
+ * few rows stay in its cache.  Row-stages whose stencil reaches into the
+ * neighbouring slab are skipped and, after one barrier, the thread above each
+ * slab edge finishes that edge's diamond (stage i on the 2i rows around the
+ * edge) stage by stage.  Each row still receives its stages in order, so all
+ * schedules apply the same operations in the same order to every component
+ * and give bit-identical results.  Slabs need at least 2s rows.
+ */
 static void *solve_thread(void *argp)
 {
   thread_arg *ta = (thread_arg *) argp;
@@ -340,9 +503,9 @@ static void *solve_thread(void *argp)
   const int lo = id < r ? id * (q + 1) : r * (q + 1) + (id - r) * q;
   const int hi = lo + (id < r ? q + 1 : q);
   double hA[ORK_MAX_STAGES][ORK_MAX_STAGES], hb[ORK_MAX_STAGES], hbh[ORK_MAX_STAGES];
-  double *y = x->y, *dy = x->dy, *err = x->err;
+  double *y = x->y, *dy = x->dy;
   double t = x->t0, h;
-  int acc = 0, rej = 0, i, j, l;
+  int acc = 0, rej = 0, i, j;
 
   /* tools.c:25-36 (H_INIT unset); step_limit <= 0 means H/0 = +inf */
   {
@@ -364,51 +527,46 @@ static void *solve_thread(void *argp)
       hbh[i] = h * x->bh[i];
     }
 
-    for (j = lo; j < hi; j++)   /* block-inline.h:253-272 */
+    if (x->rows <= 0)
     {
-      const double F = eval_at(x, j, y);
-      const double Y = y[j];
-      for (l = 1; l < s; l++)
-        x->w[l][j] = Y + hA[l][0] * F;
-      dy[j] = hb[0] * F;
-      err[j] = hbh[0] * F;
-    }
-    if (P > 1)
-      pthread_barrier_wait(&x->bar);
-
-    for (i = 1; i < s - 1; i++) /* block-inline.h:276-294 */
-    {
-      const double *wi = x->w[i];
-      for (j = lo; j < hi; j++)
+      for (i = 0; i < s; i++)
       {
-        const double F = eval_at(x, j, wi);
-        for (l = i + 1; l < s; l++)
-          x->w[l][j] += hA[l][i] * F;
-        dy[j] += hb[i] * F;
-        err[j] += hbh[i] * F;
+        stage_range(x, i, hA, hb, hbh, lo, hi, &emax);
+        if (P > 1 && i < s - 1)
+          pthread_barrier_wait(&x->bar);
       }
+    }
+    else
+    {
+      /* slab of grid rows [r0, r1) of this thread; a row-stage (i, k) whose
+         stencil reaches the neighbouring slab is "boundary": rows r0..r0+i-1
+         below the top edge and r1-i..r1-1 above the bottom edge (no edge at
+         the grid's own first and last row) */
+      const int N = x->p->grid_n, rowc = 2 * N;
+      const int qr = N / P, rr = N % P;
+      const int r0 = id < rr ? id * (qr + 1) : rr * (qr + 1) + (id - rr) * qr;
+      const int r1 = r0 + (id < rr ? qr + 1 : qr);
+      const int top = id > 0, bot = id < P - 1;
+      int tau;
+      /* phase 1: diagonal sweep over the slab, stage i on row tau - i */
+      for (tau = r0; tau < r1 + s - 1; tau++)
+        for (i = 0; i < s; i++)
+        {
+          const int k = tau - i;
+          if (k < r0 + (top ? i : 0) || k > r1 - 1 - (bot ? i : 0))
+            continue;
+          stage_range(x, i, hA, hb, hbh, k * rowc, (k + 1) * rowc, &emax);
+        }
       if (P > 1)
         pthread_barrier_wait(&x->bar);
-    }
-
-    {                           /* block-inline.h:298-320, tools.h:280-288 */
-      const double *wl = x->w[s - 1];
-      i = s - 1;
-      for (j = lo; j < hi; j++)
-      {
-        const double F = eval_at(x, j, wl);
-        double yold, div;
-        dy[j] += hb[i] * F;
-        err[j] += hbh[i] * F;
-        yold = y[j];
-        y[j] += dy[j];
-        dy[j] = yold;
-        div = fmax(fabs(y[j]), fabs(yold));
-        if (div == 0.0)
-          emax = 1.7E308;
-        else
-          emax = fmax(emax, fabs(err[j]) / div);
-      }
+      /* phase 2: the boundary diamond below this slab's bottom edge, stage
+         by stage (its rows: r1-i .. r1+i-1 for stage i) */
+      if (bot)
+        for (i = 1; i < s; i++)
+        {
+          const int k0 = r1 - i, k1 = r1 + i;
+          stage_range(x, i, hA, hb, hbh, k0 * rowc, k1 * rowc, &emax);
+        }
     }
 
     /* Every thread combines the per-thread maxima in thread order, so all
@@ -459,6 +617,15 @@ int ork_solve(const ork_problem *p, const ork_tableau *tab, double t0, double te
               const double *y0, double *y, double tol, int step_limit,
               ork_stats *stats, double *h_trace, int trace_cap, int nthreads)
 {
+  return ork_solve_pipelined(p, tab, t0, te, y0, y, tol, step_limit, stats, h_trace,
+                             trace_cap, nthreads, 0);
+}
+
+int ork_solve_pipelined(const ork_problem *p, const ork_tableau *tab, double t0, double te,
+                        const double *y0, double *y, double tol, int step_limit,
+                        ork_stats *stats, double *h_trace, int trace_cap, int nthreads,
+                        int rows)
+{
   solve_ctx x;
   thread_arg *args;
   pthread_t *tids;
@@ -478,6 +645,8 @@ int ork_solve(const ork_problem *p, const ork_tableau *tab, double t0, double te
     nthreads = 1;
   if (nthreads > p->n)
     nthreads = p->n;
+  if (p->kind == ORK_BRUSS2D_MIX && rows > 0 && nthreads > p->grid_n / (2 * tab->s))
+    nthreads = p->grid_n / (2 * tab->s) > 0 ? p->grid_n / (2 * tab->s) : 1;
 
   memset(&x, 0, sizeof(x));
   x.p = p;
@@ -491,6 +660,7 @@ int ork_solve(const ork_problem *p, const ork_tableau *tab, double t0, double te
   x.tol = tol;
   x.coef = p->kind == ORK_BRUSS2D_MIX ? bruss_coef(p) : 0.0;
   x.stats = stats;
+  x.rows = (p->kind == ORK_BRUSS2D_MIX && rows > 0) ? 1 : 0;
   x.h_trace = h_trace;
   x.trace_cap = trace_cap;
   memcpy(x.A, tab->A, sizeof(x.A));

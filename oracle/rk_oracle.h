@@ -72,6 +72,16 @@ int ork_solve(const ork_problem *p, const ork_tableau *tab, double t0, double te
               const double *y0, double *y, double tol, int step_limit,
               ork_stats *stats, double *h_trace, int trace_cap, int nthreads);
 
+/* Same step loop with the pipelined schedule (BRUSS2D-MIX, rows > 0): each
+   thread sweeps a slab of grid rows diagonally, slab edges are finished after
+   one barrier; bit-identical results, the stage vectors of a few rows stay in
+   cache (the idea of the reference's PipeD variants).  rows <= 0 selects the
+   D schedule.  Threads are limited to grid_n / (2 s). */
+int ork_solve_pipelined(const ork_problem *p, const ork_tableau *tab, double t0, double te,
+                        const double *y0, double *y, double tol, int step_limit,
+                        ork_stats *stats, double *h_trace, int trace_cap, int nthreads,
+                        int rows);
+
 #ifdef __cplusplus
 }
 #endif

@@ -101,8 +101,9 @@ def eval_all(kind, y, grid_n=0, alpha=0.0, lv_r=None, lv_a=None):
 
 
 def solve(kind, y0, method, t0, te, tol, step_limit=0, grid_n=0, alpha=0.0, lv_r=None,
-          lv_a=None, threads=1, trace=False):
-    """Returns (y, dict(steps_acc, steps_rej, t, h, h_trace))."""
+          lv_a=None, threads=1, trace=False, rows=0):
+    """Returns (y, dict(steps_acc, steps_rej, t, h, h_trace)).  rows > 0 selects the
+    pipelined schedule (BRUSS2D-MIX) with blocks of that many grid rows."""
     y0 = np.ascontiguousarray(y0, dtype=np.float64)
     p, keep = _problem(kind, y0.size, grid_n, alpha, lv_r, lv_a)
     t = Tableau()
@@ -112,10 +113,12 @@ def solve(kind, y0, method, t0, te, tol, step_limit=0, grid_n=0, alpha=0.0, lv_r
     st = Stats()
     cap = 1 << 20 if trace else 0
     tr = np.zeros(cap) if trace else None
-    rc = _lib.ork_solve(ctypes.byref(p), ctypes.byref(t), ctypes.c_double(t0), ctypes.c_double(te),
-                        y0.ctypes.data_as(ctypes.c_void_p), y.ctypes.data_as(ctypes.c_void_p),
-                        ctypes.c_double(tol), int(step_limit), ctypes.byref(st),
-                        tr.ctypes.data_as(ctypes.c_void_p) if trace else None, cap, int(threads))
+    rc = _lib.ork_solve_pipelined(ctypes.byref(p), ctypes.byref(t), ctypes.c_double(t0),
+                                  ctypes.c_double(te), y0.ctypes.data_as(ctypes.c_void_p),
+                                  y.ctypes.data_as(ctypes.c_void_p), ctypes.c_double(tol),
+                                  int(step_limit), ctypes.byref(st),
+                                  tr.ctypes.data_as(ctypes.c_void_p) if trace else None, cap,
+                                  int(threads), int(rows))
     if rc != 0:
         raise RuntimeError(f"ork_solve failed: {rc}")
     out = dict(steps_acc=st.steps_acc, steps_rej=st.steps_rej, t=st.t, h=st.h)

@@ -48,6 +48,19 @@ def test_threaded_oracle_is_bit_identical(oracle):
     np.testing.assert_array_equal(a, b)
 
 
+@pytest.mark.parametrize("method,threads", [("DOPRI54", 1), ("DOPRI54", 3), ("DOPRI87", 2),
+                                            ("RKF23", 4)])
+def test_pipelined_oracle_is_bit_identical(oracle, method, threads):
+    """The cache-blocked (pipelined) schedule used as the CPU baseline gives the D schedule's bits."""
+    y0 = oracle.bruss_start(48)
+    a, sa = oracle.solve(oracle.BRUSS2D_MIX, y0, method, 0.0, 0.2, 1e-6, grid_n=48, alpha=2e-3,
+                         threads=1)
+    b, sb = oracle.solve(oracle.BRUSS2D_MIX, y0, method, 0.0, 0.2, 1e-6, grid_n=48, alpha=2e-3,
+                         threads=threads, rows=1)
+    assert sa == sb
+    np.testing.assert_array_equal(a, b)
+
+
 def test_oracle_rejects_bad_arguments(oracle):
     y0 = oracle.bruss_start(8)
     with pytest.raises(RuntimeError):   # fixed step size needs a step limit
