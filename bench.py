@@ -13,13 +13,15 @@ attempted RK step (accepted or rejected) over all n components.
   roofline algorithmic bytes (16 n per attempted step: read y, write y) over the
            launch time, against the measured HBM copy bandwidth; the FP64
            pipe, not HBM, bounds this kernel, so "fp64" reports its share too
-  cpu_baseline the oracle port (the reference's D step loop restated in C,
-           pthreads over every host core) on a bounded sample of the same steps
+  cpu_baseline the oracle port (the reference's step loop restated in C in its
+           fastest form, the low-storage pipelined schedule of PipeD4ls, pthreads
+           over every host core) on a bounded sample of the same steps
 
 --gpus N runs N independent replicas (the path does not shard); value is
 the sum over replicas (N K steps over the slowest replica's time).
---impl reference times the reference's CPU algorithm (the oracle port, every
-host thread) on the same workload instead.
+--impl reference times the reference's CPU algorithm (the oracle port in the
+schedule of its fastest pthreads variant, every host thread) on the same
+workload instead.
 """
 import argparse
 import json
@@ -153,20 +155,29 @@ def _max_over_ranks(x, dist, device=None):
     return float(t.item())
 
 
+# the CPU port's schedule: the low-storage pipelined one (the reference's
+# fastest pthreads variant, PipeD4ls); bit-identical to the D schedule
+PORT_SCHEDULE = "low-storage pipelined schedule (PipeD4ls form)"
+
+
+def port_solve(rk_oracle, y0, tol, steps, threads, grid_n=GRID_N, alpha=ALPHA, t0=None, te=None):
+    return rk_oracle.solve(rk_oracle.BRUSS2D_MIX, y0, "DOPRI54", T0 if t0 is None else t0,
+                           TE if te is None else te, tol, step_limit=steps, grid_n=grid_n,
+                           alpha=alpha, threads=threads, rows=1)
+
+
 def cpu_baseline_port(threads, target_s=12.0, max_steps=400):
-    """Time the oracle port (reference D loop in C, pthreads) on the full-size
-    problem: as many steps as fit in about target_s, at least 2."""
+    """Time the oracle port (the reference's step loop in C, pthreads) on the
+    full-size problem: as many steps as fit in about target_s, at least 2."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import rk_oracle
     y0 = rk_oracle.bruss_start(GRID_N)
     t = time.perf_counter()
-    rk_oracle.solve(rk_oracle.BRUSS2D_MIX, y0, "DOPRI54", T0, TE, TOL, step_limit=1,
-                    grid_n=GRID_N, alpha=ALPHA, threads=threads)
+    port_solve(rk_oracle, y0, TOL, 1, threads)
     one = time.perf_counter() - t
     steps = int(max(2, min(max_steps, target_s / max(one, 1e-6))))
     t = time.perf_counter()
-    _, st = rk_oracle.solve(rk_oracle.BRUSS2D_MIX, y0, "DOPRI54", T0, TE, TOL, step_limit=steps,
-                            grid_n=GRID_N, alpha=ALPHA, threads=threads)
+    _, st = port_solve(rk_oracle, y0, TOL, steps, threads)
     dt = time.perf_counter() - t
     done = st["steps_acc"] + st["steps_rej"]
     return done / dt, done, dt
@@ -183,14 +194,12 @@ def run_reference(args):
     import rk_oracle
     y0 = rk_oracle.bruss_start(GRID_N)
     t = time.perf_counter()
-    rk_oracle.solve(rk_oracle.BRUSS2D_MIX, y0, "DOPRI54", T0, TE, TOL, step_limit=max(1, args.warmup),
-                    grid_n=GRID_N, alpha=ALPHA, threads=threads)
+    port_solve(rk_oracle, y0, TOL, max(1, args.warmup), threads)
     warm = time.perf_counter() - t
     per = warm / max(1, args.warmup)
     k = max(2, min(args.steps, int(150.0 / max(per, 1e-6))))
     t = time.perf_counter()
-    _, st = rk_oracle.solve(rk_oracle.BRUSS2D_MIX, y0, "DOPRI54", T0, TE, TOL, step_limit=k,
-                            grid_n=GRID_N, alpha=ALPHA, threads=threads)
+    _, st = port_solve(rk_oracle, y0, TOL, k, threads)
     dt = time.perf_counter() - t
     k = st["steps_acc"] + st["steps_rej"]
     v = k / dt
@@ -202,7 +211,8 @@ def run_reference(args):
         "config": {"workload": "bruss2d-mix N=2000 n=8e6 DOPRI54 tol=1e-6 t=[0,0.5]",
                    "grid_n": GRID_N, "alpha": ALPHA, "method": "DOPRI54"},
         "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
-                         "sample": f"first {k} steps of the N=2000 solve, D step loop, {threads} pthreads"},
+                         "sample": f"first {k} steps of the N=2000 solve, {PORT_SCHEDULE}, "
+                                   f"{threads} pthreads"},
         "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -325,7 +335,7 @@ def run_ours(args):
         v, k, dt = cpu_baseline_port(threads)
         line["cpu_baseline"] = {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
                                 "sample": f"first {k} steps of the same N=2000 solve ({dt:.1f} s), "
-                                          f"D step loop restated in C, {threads} pthreads"}
+                                          f"{PORT_SCHEDULE}, {threads} pthreads"}
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -426,8 +436,8 @@ def run_batched(args):
             acc += workloads.estimated_work(sample[k])
         def one(k):
             d = sample[k]
-            return rk_oracle.solve(rk_oracle.BRUSS2D_MIX, y0s[k], "DOPRI54", 0.0, 0.5, d["tol"],
-                                   grid_n=d["grid_n"], alpha=d["alpha"], threads=1)
+            return port_solve(rk_oracle, y0s[k], d["tol"], 0, 1, grid_n=d["grid_n"],
+                              alpha=d["alpha"], t0=0.0, te=0.5)
         t = time.perf_counter()
         with cf.ThreadPoolExecutor(threads) as ex:
             outs = list(ex.map(one, picked))

@@ -304,7 +304,10 @@ typedef struct
   double *y, *w[ORK_MAX_STAGES], *dy, *err;
   double *slot;                 /* per-thread err_max, padded */
   pthread_barrier_t bar;
-  int rows;                     /* > 0: pipelined schedule with blocks of this many rows */
+  int rows;                     /* > 0: low-storage pipelined schedule */
+  double *edge[ORK_MAX_STAGES + 1];   /* per slab edge: 2s rows of w_1..w_{s-1}, err */
+  double *ls_work;              /* per thread: one row of f, then the rings */
+  size_t ls_per_thread;
   ork_stats *stats;
   double *h_trace;
   int trace_cap;
@@ -482,17 +485,141 @@ static void stage_range(solve_ctx *x, int i, double hA[][ORK_MAX_STAGES], const 
 }
 
 /*
+ * Low-storage pipelined form (BRUSS2D-MIX).  y and dy are full vectors; the
+ * argument vectors w_1 .. w_{s-1} and err are kept per grid row: a row near a
+ * slab edge (within s rows of it) lives in that edge's store, every other row
+ * in a ring of the owning thread (l + 2 rows for w_l, s rows for err), since
+ * in the diagonal sweep row k of w_l is written at sweep step k and last read
+ * at step k + l + 1, and row k of err is last read at step k + s - 1.
+ */
+typedef struct
+{
+  solve_ctx *x;
+  int id, r0, r1, top, bot;
+  double *ring[ORK_MAX_STAGES + 1];   /* [1 .. s-1]: w_l, [s]: err */
+  int ring_rows[ORK_MAX_STAGES + 1];
+  double *F;                          /* one row of f values */
+} ls_thread;
+
+/* row k of vector v (1 .. s-1: w_v, s: err) */
+static double *ls_row(const ls_thread *T, int v, int k)
+{
+  const solve_ctx *x = T->x;
+  const int s = x->s, rowc = 2 * x->p->grid_n;
+  if (T->top && k < T->r0 + s)
+    return x->edge[v] + ((size_t) (T->id - 1) * 2 * s + (size_t) (k - (T->r0 - s))) * rowc;
+  if (T->bot && k >= T->r1 - s)
+    return x->edge[v] + ((size_t) T->id * 2 * s + (size_t) (k - (T->r1 - s))) * rowc;
+  return T->ring[v] + (size_t) (k % T->ring_rows[v]) * rowc;
+}
+
+/* bruss_comp on one grid row, from three row pointers (bruss2d-mix.c:66-206);
+   interior columns in a branch-free loop over (u, v) pairs */
+static void bruss_row(int N, double coef, const double *upr, const double *cr,
+                      const double *dnr, double *F)
+{
+  const int last = N - 1;
+  int j;
+  for (j = 0; j < N; j += last > 0 ? last : 1)   /* first and last column */
+  {
+    const int c = 2 * j, in = j == 0 ? c + 2 : c - 2;
+    const double u = cr[c], v = cr[c + 1];
+    const double lu = (upr[c] + dnr[c] + 2.0 * cr[in]) - 4.0 * u;
+    const double lv = (upr[c + 1] + dnr[c + 1] + 2.0 * cr[in + 1]) - 4.0 * v;
+    F[c] = (1.0 + u * u * v - 4.4 * u) + coef * lu;
+    F[c + 1] = (3.4 * u - u * u * v) + coef * lv;
+    if (last == 0)
+      break;
+  }
+  for (j = 1; j < last; j++)
+  {
+    const int c = 2 * j;
+    const double u = cr[c], v = cr[c + 1];
+    const double lu = (upr[c] + dnr[c] + cr[c - 2] + cr[c + 2]) - 4.0 * u;
+    const double lv = (upr[c + 1] + dnr[c + 1] + cr[c - 1] + cr[c + 3]) - 4.0 * v;
+    F[c] = (1.0 + u * u * v - 4.4 * u) + coef * lu;
+    F[c + 1] = (3.4 * u - u * u * v) + coef * lv;
+  }
+}
+
+/* stage i on grid row k: stage_first / stage_mid / stage_last restricted to
+   one row, with the same operations in the same order */
+static void ls_row_stage(ls_thread *T, int i, int k, double hA[][ORK_MAX_STAGES],
+                         const double *hb, const double *hbh, double *emax)
+{
+  solve_ctx *x = T->x;
+  const int s = x->s, N = x->p->grid_n, rowc = 2 * N;
+  const int ku = k == 0 ? k + 1 : k - 1, kd = k == N - 1 ? k - 1 : k + 1;
+  double *y = x->y + (size_t) k * rowc, *dy = x->dy + (size_t) k * rowc;
+  double *F = T->F, *err = ls_row(T, s, k);
+  int c, l;
+  if (i == 0)
+    bruss_row(N, x->coef, x->y + (size_t) ku * rowc, y, x->y + (size_t) kd * rowc, F);
+  else
+    bruss_row(N, x->coef, ls_row(T, i, ku), ls_row(T, i, k), ls_row(T, i, kd), F);
+  if (i == 0)
+  {
+    for (l = 1; l < s; l++)
+    {
+      const double al = hA[l][0];
+      double *wl = ls_row(T, l, k);
+      for (c = 0; c < rowc; c++)
+        wl[c] = y[c] + al * F[c];
+    }
+    for (c = 0; c < rowc; c++)
+    {
+      dy[c] = hb[0] * F[c];
+      err[c] = hbh[0] * F[c];
+    }
+  }
+  else if (i < s - 1)
+  {
+    for (l = i + 1; l < s; l++)
+    {
+      const double al = hA[l][i];
+      double *wl = ls_row(T, l, k);
+      for (c = 0; c < rowc; c++)
+        wl[c] += al * F[c];
+    }
+    for (c = 0; c < rowc; c++)
+    {
+      dy[c] += hb[i] * F[c];
+      err[c] += hbh[i] * F[c];
+    }
+  }
+  else
+  {
+    for (c = 0; c < rowc; c++)
+    {
+      double yold, div;
+      dy[c] += hb[i] * F[c];
+      err[c] += hbh[i] * F[c];
+      yold = y[c];
+      y[c] += dy[c];
+      dy[c] = yold;
+      div = fmax(fabs(y[c]), fabs(yold));
+      if (div == 0.0)
+        *emax = 1.7E308;
+      else
+        *emax = fmax(*emax, fabs(err[c]) / div);
+    }
+  }
+}
+
+/*
  * The step of one thread.  Schedule D (x->rows == 0): stage by stage over the
  * thread's block of components, a barrier between stages (pthreads/D.c).
- * Pipelined schedule (x->rows != 0, BRUSS2D-MIX; the idea of the reference's
- * PipeD variants, seq/PipeD.c:62-124): every thread owns a slab of grid rows
- * and sweeps it diagonally, stage i on row tau - i, so the stage vectors of a
- * few rows stay in its cache.  Row-stages whose stencil reaches into the
- * neighbouring slab are skipped and, after one barrier, the thread above each
- * slab edge finishes that edge's diamond (stage i on the 2i rows around the
- * edge) stage by stage.  Each row still receives its stages in order, so all
- * schedules apply the same operations in the same order to every component
- * and give bit-identical results.  Slabs need at least 2s rows.
+ * Low-storage pipelined schedule (x->rows != 0, BRUSS2D-MIX; the reference's
+ * PipeD4ls idea, pthreads/PipeD4ls.c, seq/PipeDls.c:49-131): every thread owns
+ * a slab of grid rows and sweeps it diagonally, stage i on row tau - i, with
+ * the argument vectors and err in row rings (ls_row), so the working set of a
+ * thread stays in its cache and only y and dy stream through memory.
+ * Row-stages whose stencil reaches into the neighbouring slab are skipped
+ * and, after one barrier, the thread above each slab edge finishes that edge's
+ * diamond (stage i on the 2i rows around the edge) stage by stage.  Each row
+ * still receives its stages in order, so all schedules apply the same
+ * operations in the same order to every component and give bit-identical
+ * results.  Slabs need at least 2s rows.
  */
 static void *solve_thread(void *argp)
 {
@@ -506,6 +633,31 @@ static void *solve_thread(void *argp)
   double *y = x->y, *dy = x->dy;
   double t = x->t0, h;
   int acc = 0, rej = 0, i, j;
+  ls_thread T;
+
+  memset(&T, 0, sizeof(T));
+  if (x->rows > 0)
+  {
+    /* slab of grid rows [r0, r1) of this thread and its rings */
+    const int N = x->p->grid_n, P_ = x->nthreads, rowc = 2 * N;
+    const int qr = N / P_, rr = N % P_;
+    T.x = x;
+    T.id = id;
+    T.r0 = id < rr ? id * (qr + 1) : rr * (qr + 1) + (id - rr) * qr;
+    T.r1 = T.r0 + (id < rr ? qr + 1 : qr);
+    T.top = id > 0;
+    T.bot = id < P_ - 1;
+    T.F = x->ls_work + (size_t) id * x->ls_per_thread;
+    {
+      double *at = T.F + rowc;
+      for (i = 1; i <= s; i++)
+      {
+        T.ring_rows[i] = i < s ? i + 2 : s;
+        T.ring[i] = at;
+        at += (size_t) T.ring_rows[i] * rowc;
+      }
+    }
+  }
 
   /* tools.c:25-36 (H_INIT unset); step_limit <= 0 means H/0 = +inf */
   {
@@ -538,15 +690,10 @@ static void *solve_thread(void *argp)
     }
     else
     {
-      /* slab of grid rows [r0, r1) of this thread; a row-stage (i, k) whose
-         stencil reaches the neighbouring slab is "boundary": rows r0..r0+i-1
-         below the top edge and r1-i..r1-1 above the bottom edge (no edge at
-         the grid's own first and last row) */
-      const int N = x->p->grid_n, rowc = 2 * N;
-      const int qr = N / P, rr = N % P;
-      const int r0 = id < rr ? id * (qr + 1) : rr * (qr + 1) + (id - rr) * qr;
-      const int r1 = r0 + (id < rr ? qr + 1 : qr);
-      const int top = id > 0, bot = id < P - 1;
+      /* a row-stage (i, k) whose stencil reaches the neighbouring slab is
+         deferred: rows r0 .. r0+i-1 below the top edge and r1-i .. r1-1
+         above the bottom edge (no edge at the grid's own first and last row) */
+      const int r0 = T.r0, r1 = T.r1, top = T.top, bot = T.bot;
       int tau;
       /* phase 1: diagonal sweep over the slab, stage i on row tau - i */
       for (tau = r0; tau < r1 + s - 1; tau++)
@@ -555,18 +702,16 @@ static void *solve_thread(void *argp)
           const int k = tau - i;
           if (k < r0 + (top ? i : 0) || k > r1 - 1 - (bot ? i : 0))
             continue;
-          stage_range(x, i, hA, hb, hbh, k * rowc, (k + 1) * rowc, &emax);
+          ls_row_stage(&T, i, k, hA, hb, hbh, &emax);
         }
       if (P > 1)
         pthread_barrier_wait(&x->bar);
-      /* phase 2: the boundary diamond below this slab's bottom edge, stage
-         by stage (its rows: r1-i .. r1+i-1 for stage i) */
+      /* phase 2: the deferred diamond around this slab's bottom edge, stage
+         by stage (stage i on rows r1-i .. r1+i-1) */
       if (bot)
         for (i = 1; i < s; i++)
-        {
-          const int k0 = r1 - i, k1 = r1 + i;
-          stage_range(x, i, hA, hb, hbh, k0 * rowc, k1 * rowc, &emax);
-        }
+          for (j = r1 - i; j < r1 + i; j++)
+            ls_row_stage(&T, i, j, hA, hb, hbh, &emax);
     }
 
     /* Every thread combines the per-thread maxima in thread order, so all
@@ -669,7 +814,36 @@ int ork_solve_pipelined(const ork_problem *p, const ork_tableau *tab, double t0,
   for (i = 0; i < s; i++)       /* seq/D.c:40-41 */
     x.bh[i] = tab->b[i] - tab->b_hat[i];
 
-  work = (double *) malloc((size_t) (s + 1) * (size_t) p->n * sizeof(double));
+  if (x.rows > 0)
+  {
+    /* dy as a full vector; per thread one row of f and the rings; per slab
+       edge 2s rows of w_1 .. w_{s-1} and err */
+    const size_t rowc = 2 * (size_t) p->grid_n, edges = (size_t) nthreads - 1;
+    size_t ring_rows = 1 + (size_t) s, edge_sz = edges * 2 * (size_t) s * rowc;
+    for (i = 1; i < s; i++)
+      ring_rows += (size_t) i + 2;
+    x.ls_per_thread = ring_rows * rowc;
+    work = (double *) malloc(((size_t) p->n + (size_t) nthreads * x.ls_per_thread
+                              + (size_t) s * edge_sz) * sizeof(double));
+    if (work)
+    {
+      x.dy = work;
+      x.ls_work = work + p->n;
+      for (i = 1; i <= s; i++)
+        x.edge[i] = x.ls_work + (size_t) nthreads * x.ls_per_thread + (size_t) (i - 1) * edge_sz;
+    }
+  }
+  else
+  {
+    work = (double *) malloc((size_t) (s + 1) * (size_t) p->n * sizeof(double));
+    if (work)
+    {
+      for (i = 1; i < s; i++)
+        x.w[i] = work + (size_t) (i - 1) * p->n;
+      x.dy = work + (size_t) (s - 1) * p->n;
+      x.err = work + (size_t) s * p->n;
+    }
+  }
   x.slot = (double *) calloc((size_t) nthreads * 16, sizeof(double));
   args = (thread_arg *) calloc((size_t) nthreads, sizeof(thread_arg));
   tids = (pthread_t *) calloc((size_t) nthreads, sizeof(pthread_t));
@@ -681,10 +855,6 @@ int ork_solve_pipelined(const ork_problem *p, const ork_tableau *tab, double t0,
     free(tids);
     return -2;
   }
-  for (i = 1; i < s; i++)
-    x.w[i] = work + (size_t) (i - 1) * p->n;
-  x.dy = work + (size_t) (s - 1) * p->n;
-  x.err = work + (size_t) s * p->n;
   x.y = y;
   memcpy(y, y0, (size_t) p->n * sizeof(double));
 
