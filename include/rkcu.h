@@ -138,6 +138,19 @@ int rkcu_advance(rkcu_solver *s, int max_steps);
 int rkcu_query(rkcu_solver *s, rkcu_stats *stats);
 int rkcu_get_y(rkcu_solver *s, double *y, int y_on_device);
 
+/* Per-step trace, the device counterpart of the reference's -DDUMP output
+   (step_control in include/tools.h:239-256 prints t, h and the candidate y of
+   every attempted step).  set_trace reserves room for the first `capacity`
+   attempted steps after each rkcu_begin (capacity 0 turns tracing off); with_y
+   also keeps each step's candidate state (capacity * n doubles).  Plain
+   FP64 form only (RKCU_VARIANT_D, not RKCU_MIXED): RKCU_ERR_INVALID otherwise.
+   get_trace copies the recorded steps: t[k], h[k] (the step's start and size),
+   err[k] (its error max) and y[k * n ..] (host arrays; any may be NULL) for k <
+   min(capacity, recorded), and sets *count to the number recorded. */
+int rkcu_set_trace(rkcu_solver *s, int capacity, int with_y);
+int rkcu_get_trace(rkcu_solver *s, double *t, double *h, double *err, double *y, int capacity,
+                   int *count);
+
 /* The device stream the solver runs on (cudaStream_t), for event timing. */
 void *rkcu_stream(rkcu_solver *s);
 /* Number of kernels this solver has launched so far. */

@@ -56,6 +56,7 @@ EXPORTS = (
     "rkcu_batch_footprint", "rkcu_batch_create", "rkcu_batch_destroy", "rkcu_batch_add",
     "rkcu_batch_run", "rkcu_batch_finished", "rkcu_batch_take", "rkcu_batch_tune",
     "rkcu_batch_set_tuning", "rkcu_batch_get_tuning", "rkcu_batch_info", "rkcu_batch_stream",
+    "rkcu_set_trace", "rkcu_get_trace",
 )
 
 
@@ -133,6 +134,8 @@ def load():
     lib.rkcu_step_size.argtypes = [D, D, D, I, P(I)]
     lib.rkcu_step_sizes_device.argtypes = [V, V, I, D, I, V, V]
     lib.rkcu_run.argtypes = [V, I, P(Stats)]
+    lib.rkcu_set_trace.argtypes = [V, I, I]
+    lib.rkcu_get_trace.argtypes = [V, V, V, V, V, I, P(I)]
     LL = ctypes.c_longlong
     lib.rkcu_batch_footprint.restype = LL
     lib.rkcu_batch_footprint.argtypes = [P(Problem), I]
@@ -358,6 +361,24 @@ class Solver:
         _check(self._lib.rkcu_get_y(self._h, _ptr(y), 0), "rkcu_get_y")
         return y
 
+    def set_trace(self, capacity, with_y=False):
+        """Record the first `capacity` attempted steps after each begin: t, h,
+        error max and, with_y, each step's candidate state (rkcu_set_trace)."""
+        _check(self._lib.rkcu_set_trace(self._h, int(capacity), 1 if with_y else 0), "rkcu_set_trace")
+        self._trace = (int(capacity), bool(with_y))
+
+    def trace(self):
+        """The recorded steps: dict of t, h, err arrays and y (steps x n) or None."""
+        cap, with_y = getattr(self, "_trace", (0, False))
+        t, h, e = np.empty(cap), np.empty(cap), np.empty(cap)
+        y = np.empty((cap, self.problem.n)) if with_y else None
+        cnt = ctypes.c_int(0)
+        _check(self._lib.rkcu_get_trace(self._h, _ptr(t), _ptr(h), _ptr(e),
+                                        _ptr(y) if y is not None else None, cap, ctypes.byref(cnt)),
+               "rkcu_get_trace")
+        k = cnt.value
+        return {"t": t[:k], "h": h[:k], "err": e[:k], "y": y[:k] if y is not None else None}
+
     def inject_wait_timeout(self, extra_arrivals):
         """Test hook: see rkcu_debug_inject_wait_timeout in include/rkcu.h."""
         _check(self._lib.rkcu_debug_inject_wait_timeout(self._h, int(extra_arrivals)),
@@ -391,6 +412,27 @@ class Solver:
 
     def __exit__(self, *a):
         self.close()
+
+
+def write_dump(path, trace):
+    """Write a trace in the reference's DUMP file format (include/tools.h:239-256):
+    one line per attempted step, t and h then every component of the candidate
+    state, each as %.20e, tab-separated."""
+    with open(path, "w") as f:
+        f.write(dump_text(trace))
+
+
+def dump_text(trace):
+    """The DUMP file contents of a trace (see write_dump)."""
+    ys = trace["y"]
+    if ys is None:
+        raise ValueError("the trace holds no states (set_trace(..., with_y=True))")
+    out = []
+    for k in range(len(trace["t"])):
+        out.append("%.20e\t%.20e" % (trace["t"][k], trace["h"][k]))
+        out.append("".join("\t%.20e" % v for v in ys[k].tolist()))
+        out.append("\n")
+    return "".join(out)
 
 
 def footprint(problem, stages=7):

@@ -5,6 +5,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <vector>
 #include <new>
 
 #include "rkcu.h"
@@ -82,6 +83,10 @@ struct rkcu_solver {
   DevState *st = nullptr;
   DevState *st_host = nullptr;  // pinned
   unsigned int *flags = nullptr;  // plain kernel: per-CTA stage progress
+  // per-step trace (plain form)
+  int trace_cap = 0;
+  double *trace_meta = nullptr;  // 3 doubles per step: t, h, error max
+  double2 *trace_y = nullptr;    // npairs per step, or none
   // run
   bool begun = false;
   double te = 0.0, tol = 0.0;
@@ -134,6 +139,8 @@ int rkcu_destroy(rkcu_solver *s) {
   cudaFree(s->lv_a);
   cudaFree(s->st);
   cudaFree(s->flags);
+  cudaFree(s->trace_meta);
+  cudaFree(s->trace_y);
   cudaFreeHost(s->st_host);
   if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
   delete s;
@@ -459,6 +466,9 @@ int rkcu_advance(rkcu_solver *s, int max_steps) {
   p.st = s->st;
   p.flags = s->flags;
   p.schedule = s->opt.schedule == 2 ? rkcu::kScheduleNeighbour : rkcu::kScheduleGrid;
+  p.trace_cap = s->trace_cap;
+  p.trace_meta = s->trace_meta;
+  p.trace_y = s->trace_y;
   p.bruss.N = s->prob.grid_n;
   p.bruss.coef = s->prob.problem == RKCU_PROBLEM_BRUSS2D_MIX ? bruss_coef(&s->prob) : 0.0;
   p.lvb.n = s->prob.n;
@@ -594,6 +604,77 @@ int rkcu_step_sizes_device(const double *h, const double *err, int count, double
 int rkcu_debug_inject_wait_timeout(rkcu_solver *s, int extra_arrivals) {
   if (!s || extra_arrivals < 0) return RKCU_ERR_INVALID;
   s->extra_arrivals = extra_arrivals;
+  return RKCU_OK;
+}
+
+int rkcu_set_trace(rkcu_solver *s, int capacity, int with_y) {
+  if (!s || capacity < 0) return RKCU_ERR_INVALID;
+  if (capacity > 0 &&
+      (s->opt.variant != RKCU_VARIANT_D || s->opt.precision == RKCU_MIXED))
+    return RKCU_ERR_INVALID;
+  RKCU_CK(cudaSetDevice(s->opt.device));
+  RKCU_CK(cudaStreamSynchronize(s->stream));
+  const long long old_bytes = (s->trace_meta ? 3LL * s->trace_cap * (long long)sizeof(double) : 0) +
+                              (s->trace_y ? (long long)s->trace_cap * s->npairs * sizeof(double2) : 0);
+  cudaFree(s->trace_meta);
+  cudaFree(s->trace_y);
+  s->trace_meta = nullptr;
+  s->trace_y = nullptr;
+  s->trace_cap = 0;
+  s->dev_bytes -= old_bytes;
+  if (capacity == 0) return RKCU_OK;
+  RKCU_CK(cudaMalloc(&s->trace_meta, 3 * (size_t)capacity * sizeof(double)));
+  long long bytes = 3LL * capacity * (long long)sizeof(double);
+  if (with_y) {
+    const size_t ybytes = (size_t)capacity * s->npairs * sizeof(double2);
+    cudaError_t e = cudaMalloc(&s->trace_y, ybytes);
+    if (e != cudaSuccess) {
+      cudaFree(s->trace_meta);
+      s->trace_meta = nullptr;
+      cudaGetLastError();
+      return e == cudaErrorMemoryAllocation ? RKCU_ERR_NOMEM : cuda_fail(e, "trace allocation");
+    }
+    bytes += (long long)ybytes;
+  }
+  s->trace_cap = capacity;
+  s->dev_bytes += bytes;
+  return RKCU_OK;
+}
+
+int rkcu_get_trace(rkcu_solver *s, double *t, double *h, double *err, double *y, int capacity,
+                   int *count) {
+  if (!s || capacity < 0) return RKCU_ERR_INVALID;
+  if (!s->begun) return RKCU_ERR_STATE;
+  rkcu_stats st{};
+  int rc = rkcu_query(s, &st);
+  if (rc != RKCU_OK) return rc;
+  const long long attempted = (long long)st.steps_acc + st.steps_rej;
+  const int rec = (int)(attempted < s->trace_cap ? attempted : s->trace_cap);
+  if (count) *count = rec;
+  const int k = rec < capacity ? rec : capacity;
+  if (k == 0) return RKCU_OK;
+  if (t || h || err) {
+    std::vector<double> meta(3 * (size_t)k);
+    RKCU_CK(cudaMemcpy(meta.data(), s->trace_meta, meta.size() * sizeof(double),
+                       cudaMemcpyDeviceToHost));
+    for (int i = 0; i < k; ++i) {
+      if (t) t[i] = meta[3 * i];
+      if (h) h[i] = meta[3 * i + 1];
+      if (err) err[i] = meta[3 * i + 2];
+    }
+  }
+  if (y) {
+    if (!s->trace_y) return RKCU_ERR_INVALID;
+    const size_t n = (size_t)s->prob.n;
+    if (n % 2 == 0) {
+      RKCU_CK(cudaMemcpy(y, s->trace_y, (size_t)k * n * sizeof(double), cudaMemcpyDeviceToHost));
+    } else {
+      // odd n: each stored step is padded to npairs pairs
+      for (int i = 0; i < k; ++i)
+        RKCU_CK(cudaMemcpy(y + (size_t)i * n, s->trace_y + (size_t)i * s->npairs,
+                           n * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+  }
   return RKCU_OK;
 }
 

@@ -158,6 +158,9 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(const __grid_constant__
     ErrMax em;
     {
       const int i = s - 1;
+      const int k = s_acc + s_rej;  // this step's index for the trace
+      double2 *__restrict__ ytr =
+          (P.trace_y && k < P.trace_cap) ? P.trace_y + static_cast<size_t>(k) * P.npairs : nullptr;
       const double2 *__restrict__ wl = P.w[i];
       const double bi = hb[i], bhi = hbh[i];
       const bool nzb = P.nzb[i], nzbh = P.nzbh[i];
@@ -176,6 +179,7 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(const __grid_constant__
         const double2 Y = ycur[p];
         const double2 yn = make_double2(M::add(Y.x, d.x), M::add(Y.y, d.y));
         ynew[p] = yn;
+        if (ytr) ytr[p] = yn;
         em.add(e.x, yn.x, Y.x);
         if (2 * p + 1 < P.n) em.add(e.y, yn.y, Y.y);
       }
@@ -200,6 +204,12 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(const __grid_constant__
       double t = s_t, hh = s_h;
       int acc = s_acc, rej = s_rej, cur = s_cur;
       bool host_pow = false;
+      if (blockIdx.x == 0 && P.trace_meta && acc + rej < P.trace_cap) {
+        double *m = P.trace_meta + 3 * static_cast<size_t>(acc + rej);
+        m[0] = t;
+        m[1] = hh;
+        m[2] = errmax;
+      }
       if (P.tol <= 0.0) {
         t += hh;
         ++acc;

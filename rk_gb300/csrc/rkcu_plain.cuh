@@ -29,6 +29,12 @@ struct PlainParams {
   DevState *st;
   unsigned int *flags;                // kMaxPlainGrid progress words (reset by each launch)
   int schedule;                       // kScheduleGrid or kScheduleNeighbour
+  // per-step trace (include/tools.h:239-256, -DDUMP): for attempted step k <
+  // trace_cap, trace_meta[3k..3k+2] = t, h, error max and, if trace_y is set,
+  // trace_y[k * npairs ..] = the step's candidate state
+  int trace_cap;
+  double *trace_meta;
+  double2 *trace_y;
   Bruss bruss;
   LvPairs lvp;
   LvBanded lvb;

@@ -10,8 +10,10 @@ compile-time DEFINES, run, and recorded as JSON under tests/golden/:
   y_sha256, y_first/last/min/max -- final state, bit for bit (float.hex)
   y_hex                        -- the whole final state for small systems
   y_sample                     -- every k-th component for large systems
-  h_trace                      -- h of every attempted step, from the
+  h_trace, t_trace             -- h and t of every attempted step, from the
                                   reference's -DDUMP trajectory (tools.h:239-256)
+  dump_sha256, dump_bytes      -- the DUMP file itself (t, h and the candidate
+                                  state of every step as %.20e), for small systems
 
 Run here, where the reference sources exist:
     python tests/golden/make_golden.py [--only NAME ...] [--big]
@@ -121,11 +123,15 @@ def run_case(case):
         y = np.fromfile(ybin, dtype="<f8")
         trace = None
         if dump:
-            trace = []
-            with open(os.path.join(td, "DUMP")) as f:
+            trace, ttrace = [], []
+            dpath = os.path.join(td, "DUMP")
+            with open(dpath) as f:
                 for line in f:
                     t_s, h_s = line.split("\t", 2)[:2]
                     trace.append(float(h_s))
+                    ttrace.append(float(t_s))
+            with open(dpath, "rb") as f:
+                dump_raw = f.read()
     m = re.search(r"Number of steps: (\d+) \((\d+) accepted, (\d+) rejected\)", out)
     steps, acc, rej = map(int, m.groups())
     n = y.size
@@ -158,6 +164,10 @@ def run_case(case):
         # the trace holds the h of every attempted step; a DUMP line is written
         # per step_control call (tools.h:239-256)
         rec["h_trace"] = [hx(v) for v in trace]
+        rec["t_trace"] = [hx(v) for v in ttrace]
+        if n <= FULL_Y_MAX:
+            rec["dump_sha256"] = hashlib.sha256(dump_raw).hexdigest()
+            rec["dump_bytes"] = len(dump_raw)
     return rec
 
 

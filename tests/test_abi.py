@@ -119,3 +119,22 @@ def test_correctly_rounded_pow_against_decimal(rkcu_lib):
                     np.nextafter(float(true_pow), np.inf)]
             best = min(cand, key=lambda c: abs(Decimal(c) - true_pow))
             assert v == 0.9 * best
+
+
+def test_dump_format_matches_c_printf():
+    """rk_gb300.dump_text writes the reference's DUMP lines: "%.20e" as C's printf formats it."""
+    import ctypes
+    import ctypes.util
+    import rk_gb300 as rk
+    libc = ctypes.CDLL(ctypes.util.find_library("c"))
+    rng = np.random.default_rng(11)
+    vals = np.concatenate([rng.standard_normal(300) * 10.0 ** rng.integers(-30, 30, 300),
+                           [0.0, -0.0, 1.0, 0.5, 1e-310, 1.7e308]])
+    buf = ctypes.create_string_buffer(64)
+    for v in vals:
+        libc.snprintf(buf, 64, b"%.20e", ctypes.c_double(float(v)))
+        assert ("%.20e" % v).encode() == buf.value
+    tr = {"t": np.array([0.0, 0.25]), "h": np.array([0.25, 0.125]),
+          "y": np.array([[1.0, 2.0], [3.0, 4.0]])}
+    lines = rk.dump_text(tr).splitlines()
+    assert len(lines) == 2 and lines[1].split("\t")[1] == "%.20e" % 0.125
