@@ -248,7 +248,8 @@ def run_ours(args):
     solver = rk.Solver(prob, method=args.method, precision=args.precision, device=local,
                        stream=stream.cuda_stream,
                        variant=rk.VARIANT_LOWSTORAGE if args.variant == "lowstorage" else rk.VARIANT_D,
-                       block_rows=args.block_rows, schedule=args.schedule)
+                       block_rows=args.block_rows, schedule=args.schedule,
+                       flow_skew=args.flow_skew)
     # ---- device-resident timing -------------------------------------------
     solver.begin(T0, TE, None, TOL, y0_device_ptr=y0_dev.data_ptr())
     st0 = solver.run(args.warmup)
@@ -521,6 +522,8 @@ def main():
     ap.add_argument("--variant", default="d", choices=["d", "lowstorage"],
                     help="d: stage vectors in HBM (default); lowstorage: wavefront with ring buffers")
     ap.add_argument("--block-rows", type=int, default=0)
+    ap.add_argument("--flow-skew", type=int, default=0,
+                    help="plain form, schedule 3: wavefront skew in tiles (0 = automatic)")
     ap.add_argument("--schedule", type=int, default=0,
                     help="plain form stage synchronisation: 0 auto, 1 grid barrier, 2 neighbour flags")
     ap.add_argument("--requests", type=int, default=400)

@@ -83,7 +83,10 @@ typedef struct
   int block_rows;       /* RKCU_VARIANT_LOWSTORAGE: grid rows per pipeline block (the
                            reference's BLOCKSIZE in rows, config.h:97-98); 0 = automatic */
   int schedule;         /* plain form, stage synchronisation: 0 = automatic, 1 = grid
-                           barrier after every stage, 2 = neighbour progress flags */
+                           barrier after every stage, 2 = neighbour progress flags,
+                           3 = dataflow over (stage, tile) in wavefront order */
+  int flow_skew;        /* schedule 3: tiles by which stage i trails stage i-1 in the
+                           wavefront; 0 = automatic (tiles are block_rows grid rows) */
 } rkcu_options;
 
 /* Progress of a solve: the counters of src/tools.c:62-79 plus the current t, h. */

@@ -82,7 +82,7 @@ class Options(ctypes.Structure):
                 ("step_limit", ctypes.c_int), ("device", ctypes.c_int),
                 ("stream", ctypes.c_void_p), ("wait_timeout_s", ctypes.c_double),
                 ("h_init", ctypes.c_double), ("block_rows", ctypes.c_int),
-                ("schedule", ctypes.c_int)]
+                ("schedule", ctypes.c_int), ("flow_skew", ctypes.c_int)]
 
 
 class Stats(ctypes.Structure):
@@ -285,7 +285,8 @@ class Solver:
     """One problem instance on one GPU (an rkcu_solver)."""
 
     def __init__(self, problem, method="DOPRI54", precision="exact", step_limit=0, device=0,
-                 stream=None, wait_timeout_s=10.0, variant=VARIANT_D, block_rows=0, schedule=0):
+                 stream=None, wait_timeout_s=10.0, variant=VARIANT_D, block_rows=0, schedule=0,
+                 flow_skew=0):
         lib = load()
         self._lib = lib
         self.problem = problem
@@ -300,6 +301,7 @@ class Solver:
         opt.wait_timeout_s = float(wait_timeout_s)
         opt.block_rows = int(block_rows)
         opt.schedule = int(schedule)
+        opt.flow_skew = int(flow_skew)
         self._ps = problem.cstruct()
         h = ctypes.c_void_p()
         _check(lib.rkcu_create(ctypes.byref(h), ctypes.byref(self._ps), ctypes.byref(opt)),

@@ -96,6 +96,26 @@ struct rkcu_solver {
   int extra_arrivals = 0;
 };
 
+// Tiles of the flow schedule: BRUSS2D-MIX tiles are block_rows grid rows (one
+// by default), so a stage reads one tile either side; the LV chains use tiles
+// of 2048 pairs (pairs: no neighbours; banded: one pair either side).
+static void flow_geometry(const rkcu_solver *s, int *tile, int *ntiles, int *dep) {
+  const int np = (int)s->npairs;
+  int t, d;
+  if (s->prob.problem == RKCU_PROBLEM_BRUSS2D_MIX) {
+    const int rows = s->opt.block_rows > 0 ? s->opt.block_rows : 1;
+    t = rows * s->prob.grid_n;
+    d = 1;
+  } else {
+    t = 2048;
+    d = s->prob.problem == RKCU_PROBLEM_LV_BANDED ? 1 : 0;
+  }
+  if (t > np) t = np > 0 ? np : 1;
+  *tile = t;
+  *ntiles = (np + t - 1) / t;
+  *dep = d;
+}
+
 extern "C" {
 
 void rkcu_options_default(rkcu_options *o) {
@@ -168,7 +188,7 @@ int rkcu_create(rkcu_solver **out, const rkcu_problem *prob, const rkcu_options 
   if (o.step_limit < 0) return RKCU_ERR_INVALID;
   if (!(o.wait_timeout_s > 0.0)) o.wait_timeout_s = 10.0;
   if (!(o.h_init >= 0.0)) return RKCU_ERR_INVALID;
-  if (o.schedule < 0 || o.schedule > 2) return RKCU_ERR_INVALID;
+  if (o.schedule < 0 || o.schedule > 3 || o.flow_skew < 0) return RKCU_ERR_INVALID;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= o.device || o.device < 0)
     return RKCU_ERR_NO_DEVICE;
@@ -205,8 +225,14 @@ int rkcu_create(rkcu_solver **out, const rkcu_problem *prob, const rkcu_options 
     return fail(cuda_fail(e, "cudaMalloc state"));
   if ((e = cudaMallocHost(&s->st_host, sizeof(DevState))) != cudaSuccess)
     return fail(cuda_fail(e, "cudaMallocHost"));
-  if ((e = cudaMalloc(&s->flags, sizeof(unsigned int) * rkcu::kMaxPlainGrid)) != cudaSuccess)
-    return fail(cuda_fail(e, "cudaMalloc flags"));
+  {
+    int tile = 0, ntiles = 0, dep = 0;
+    flow_geometry(s, &tile, &ntiles, &dep);
+    size_t words = rkcu::flow_words(ntiles);
+    if (words < (size_t)rkcu::kMaxPlainGrid) words = rkcu::kMaxPlainGrid;
+    if ((e = cudaMalloc(&s->flags, sizeof(unsigned int) * words)) != cudaSuccess)
+      return fail(cuda_fail(e, "cudaMalloc flags"));
+  }
   if (prob->problem == RKCU_PROBLEM_LV_BANDED) {
     const size_t np = 2 * s->npairs;
     if ((e = cudaMalloc(&s->lv_r, np * sizeof(double))) != cudaSuccess)
@@ -282,7 +308,10 @@ int rkcu_begin(rkcu_solver *s, double t0, double te, const double *y0, int y0_on
   }
   if (s->opt.variant == RKCU_VARIANT_LOWSTORAGE) {
     const int N = s->prob.grid_n;
-    int R = s->opt.block_rows > 0 ? s->opt.block_rows : (s->s <= 8 ? 32 : 16);
+    // blocks of 64 rows (32 for the 13-stage DOPRI87): fewer wavefront steps
+    // (grid barriers) per RK step than smaller blocks, still a third of the
+    // plain form's storage at N = 2000
+    int R = s->opt.block_rows > 0 ? s->opt.block_rows : (s->s <= 8 ? 64 : 32);
     if (R > N) R = N;
     while (R > 1 && (double)R * N * N >= 1099511627776.0) R /= 2;  // row division needs q N < 2^40
     const size_t need_pairs = rkcu::lowstorage_ring_pairs(s->s, R, N);
@@ -465,7 +494,13 @@ int rkcu_advance(rkcu_solver *s, int max_steps) {
   p.err = s->stage + (size_t)s->s * s->npairs;
   p.st = s->st;
   p.flags = s->flags;
-  p.schedule = s->opt.schedule == 2 ? rkcu::kScheduleNeighbour : rkcu::kScheduleGrid;
+  p.schedule = s->opt.schedule == 2   ? rkcu::kScheduleNeighbour
+               : s->opt.schedule == 3 ? rkcu::kScheduleFlow
+                                      : rkcu::kScheduleGrid;
+  flow_geometry(s, &p.flow_tile, &p.flow_ntiles, &p.flow_dep);
+  p.flow_skew = s->opt.flow_skew;  // 0: chosen at launch from the grid size
+  // the flow schedule's tile counters hold step * s + stage within a launch
+  if (p.schedule == rkcu::kScheduleFlow && p.budget > (1 << 24)) p.budget = 1 << 24;
   p.trace_cap = s->trace_cap;
   p.trace_meta = s->trace_meta;
   p.trace_y = s->trace_y;

@@ -327,6 +327,57 @@ __device__ __forceinline__ bool wait_neighbours(const unsigned int *flags, int c
   return s_ok != 0;
 }
 
+__device__ __forceinline__ unsigned int ld_acquire(const unsigned int *p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_release(unsigned int *p, unsigned int v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Dataflow tiles: after the whole CTA has written tile c, mark it with value.
+__device__ __forceinline__ void publish_tile(unsigned int *done, int c, unsigned int value) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    st_release(&done[c], value);
+  }
+}
+
+// Wait until tiles c_lo..c_hi are marked with at least target (bounded by
+// timeout_ns, as the grid barrier); the CTA may then read what they wrote.
+__device__ __forceinline__ bool wait_tiles(const unsigned int *done, int c_lo, int c_hi,
+                                           unsigned int target, DevState *st,
+                                           unsigned long long timeout_ns, int site) {
+  __shared__ int s_ok;
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    unsigned long long t0 = 0;
+    for (int c = c_lo; c <= c_hi && ok; ++c) {
+      unsigned int ns = 32;
+      while (ld_acquire(&done[c]) < target) {
+        if (t0 == 0) t0 = globaltimer_ns();
+        if (*(volatile int *)&st->error) {
+          ok = 0;
+          break;
+        }
+        if (globaltimer_ns() - t0 > timeout_ns) {
+          if (atomicCAS(&st->error, 0, 1) == 0) st->error_site = site;
+          ok = 0;
+          break;
+        }
+        __nanosleep(ns);
+        if (ns < 256) ns <<= 1;
+      }
+    }
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
 // Step-size update of include/tools.h:221-233 (AMAX 2, AMIN 0.5, ASAF 0.9),
 // with a correctly rounded pow; *host_pow flags the rare updates the host
 // finishes with the C library's pow (see step_factor_h).

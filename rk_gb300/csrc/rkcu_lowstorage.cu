@@ -12,7 +12,7 @@
 // Storage: y (two full vectors, ping-pong as in the plain form) plus ring
 // buffers: w_l keeps the blocks from tau-2l-1 to tau (2l+2 slots), dy and err
 // keep 2s-1 blocks -- 2n + (s^2 + 5s - 4) R 2N doubles instead of (s+3) n;
-// for N = 2000, R = 32, DOPRI5(4): 128 MB + 82 MB instead of 640 MB, and the
+// for N = 2000, R = 64, DOPRI5(4): 128 MB + 164 MB instead of 640 MB, and the
 // window stays in L2.  Every component sees the same operations in the same
 // order as in the plain form, so results are bit-identical to it.
 #include "rkcu.h"

@@ -52,6 +52,7 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(const __grid_constant__
   __shared__ unsigned long long s_step;
   __shared__ double s_pend_err, s_pend_h;
   __shared__ double s_wmax[kThreads / 32];
+  __shared__ unsigned int s_tk[2];
 
   const Prob &prob = problem_of<Prob>(P);
   DevState *st = P.st;
@@ -103,9 +104,12 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(const __grid_constant__
     __syncthreads();
     const double2 *__restrict__ ycur = P.y[s_cur];
     double2 *__restrict__ ynew = P.y[s_cur ^ 1];
+    const int kstep = s_acc + s_rej;  // this step's index (for the trace)
+    double2 *__restrict__ ytr =
+        (P.trace_y && kstep < P.trace_cap) ? P.trace_y + static_cast<size_t>(kstep) * P.npairs : nullptr;
 
-    // first stage (block-inline.h:253-272)
-    for (int p = p0; p < pend; p += pstep) {
+    // first stage at pair p (block-inline.h:253-272)
+    auto stage_first = [&](int p) {
       const double2 F = prob.template eval<kExact>(ycur, p);
       const double2 Y = ycur[p];
       for (int l = 1; l < s; ++l) {
@@ -119,70 +123,110 @@ __global__ void __launch_bounds__(kThreads) plain_kernel(const __grid_constant__
       }
       P.dy[p] = make_double2(M::mul(hb[0], F.x), M::mul(hb[0], F.y));
       P.err[p] = make_double2(M::mul(hbh[0], F.x), M::mul(hbh[0], F.y));
-    }
-    if (!(ok = stage_sync(P, c_lo, c_hi, ++progress, 1))) break;
-
-    // intermediate stages (block-inline.h:276-294)
-    for (int i = 1; i < s - 1; ++i) {
-      const double2 *__restrict__ wi = P.w[i];
-      const double bi = hb[i], bhi = hbh[i];
-      const bool nzb = P.nzb[i], nzbh = P.nzbh[i];
-      for (int p = p0; p < pend; p += pstep) {
-        const double2 F = prob.template eval<kExact>(wi, p);
-        for (int l = i + 1; l < s; ++l) {
-          if (!P.nzA[l * kMaxStages + i]) continue;
-          const double a = hA[l * kMaxStages + i];
-          double2 wv = P.w[l][p];
-          wv.x = M::mac(wv.x, a, F.x);
-          wv.y = M::mac(wv.y, a, F.y);
-          P.w[l][p] = wv;
-        }
-        if (nzb) {
-          double2 d = P.dy[p];
-          d.x = M::mac(d.x, bi, F.x);
-          d.y = M::mac(d.y, bi, F.y);
-          P.dy[p] = d;
-        }
-        if (nzbh) {
-          double2 e = P.err[p];
-          e.x = M::mac(e.x, bhi, F.x);
-          e.y = M::mac(e.y, bhi, F.y);
-          P.err[p] = e;
-        }
+    };
+    // intermediate stage i at pair p (block-inline.h:276-294)
+    auto stage_mid = [&](int i, int p) {
+      const double2 F = prob.template eval<kExact>(P.w[i], p);
+      for (int l = i + 1; l < s; ++l) {
+        if (!P.nzA[l * kMaxStages + i]) continue;
+        const double a = hA[l * kMaxStages + i];
+        double2 wv = P.w[l][p];
+        wv.x = M::mac(wv.x, a, F.x);
+        wv.y = M::mac(wv.y, a, F.y);
+        P.w[l][p] = wv;
       }
-      if (!(ok = stage_sync(P, c_lo, c_hi, ++progress, 2))) break;
-    }
-    if (!ok) break;
-
-    // last stage (block-inline.h:298-320) and error max (tools.h:280-288)
-    ErrMax em;
-    {
-      const int i = s - 1;
-      const int k = s_acc + s_rej;  // this step's index for the trace
-      double2 *__restrict__ ytr =
-          (P.trace_y && k < P.trace_cap) ? P.trace_y + static_cast<size_t>(k) * P.npairs : nullptr;
-      const double2 *__restrict__ wl = P.w[i];
-      const double bi = hb[i], bhi = hbh[i];
-      const bool nzb = P.nzb[i], nzbh = P.nzbh[i];
-      for (int p = p0; p < pend; p += pstep) {
-        const double2 F = prob.template eval<kExact>(wl, p);
+      if (P.nzb[i]) {
+        const double bi = hb[i];
         double2 d = P.dy[p];
-        double2 e = P.err[p];
-        if (nzb) {
-          d.x = M::mac(d.x, bi, F.x);
-          d.y = M::mac(d.y, bi, F.y);
-        }
-        if (nzbh) {
-          e.x = M::mac(e.x, bhi, F.x);
-          e.y = M::mac(e.y, bhi, F.y);
-        }
-        const double2 Y = ycur[p];
-        const double2 yn = make_double2(M::add(Y.x, d.x), M::add(Y.y, d.y));
-        ynew[p] = yn;
-        if (ytr) ytr[p] = yn;
-        em.add(e.x, yn.x, Y.x);
-        if (2 * p + 1 < P.n) em.add(e.y, yn.y, Y.y);
+        d.x = M::mac(d.x, bi, F.x);
+        d.y = M::mac(d.y, bi, F.y);
+        P.dy[p] = d;
       }
+      if (P.nzbh[i]) {
+        const double bhi = hbh[i];
+        double2 e = P.err[p];
+        e.x = M::mac(e.x, bhi, F.x);
+        e.y = M::mac(e.y, bhi, F.y);
+        P.err[p] = e;
+      }
+    };
+    // last stage at pair p (block-inline.h:298-320) and its error terms (tools.h:280-288)
+    ErrMax em;
+    auto stage_last = [&](int p) {
+      const int i = s - 1;
+      const double2 F = prob.template eval<kExact>(P.w[i], p);
+      double2 d = P.dy[p];
+      double2 e = P.err[p];
+      if (P.nzb[i]) {
+        d.x = M::mac(d.x, hb[i], F.x);
+        d.y = M::mac(d.y, hb[i], F.y);
+      }
+      if (P.nzbh[i]) {
+        e.x = M::mac(e.x, hbh[i], F.x);
+        e.y = M::mac(e.y, hbh[i], F.y);
+      }
+      const double2 Y = ycur[p];
+      const double2 yn = make_double2(M::add(Y.x, d.x), M::add(Y.y, d.y));
+      ynew[p] = yn;
+      if (ytr) ytr[p] = yn;
+      em.add(e.x, yn.x, Y.x);
+      if (2 * p + 1 < P.n) em.add(e.y, yn.y, Y.y);
+    };
+
+    if (P.schedule == kScheduleFlow) {
+      // Dataflow over (stage, tile) tickets in skewed wavefront order: tile c
+      // of stage i is ticket (c + K i) s + i, and waits only until stage i-1
+      // is complete on tiles c-dt .. c+dt (the rows its stencil reads).  With
+      // K >= dt every dependency holds a smaller ticket, and the CTA holding
+      // the smallest unfinished ticket never waits, so the schedule cannot
+      // deadlock among co-resident CTAs.  Tiles completed: done[c] =
+      // it s + i + 1 (the counters are zeroed by each launch).
+      const int nt = P.flow_ntiles, tp = P.flow_tile, K = P.flow_skew, dt = P.flow_dep;
+      unsigned int *ticket = P.flags;
+      unsigned int *done = P.flags + 2;
+      const unsigned int total = static_cast<unsigned int>(nt + K * (s - 1)) * s;
+      const unsigned int base = static_cast<unsigned int>(it) * s;
+      // the counter of the next step was last used a step ago: clear it
+      if (blockIdx.x == 0 && threadIdx.x == 0) atomicExch(&ticket[(it + 1) & 1], 0u);
+      if (threadIdx.x == 0) s_tk[0] = atomicAdd(&ticket[it & 1], 1u);
+      __syncthreads();
+      unsigned int tk = s_tk[0];
+      int slot = 0;
+      while (tk < total) {
+        // fetch the next ticket while this tile runs
+        if (threadIdx.x == 0) s_tk[slot ^ 1] = atomicAdd(&ticket[it & 1], 1u);
+        const int i = static_cast<int>(tk % s);
+        const int c = static_cast<int>(tk / s) - K * i;
+        if (c >= 0 && c < nt) {
+          if (i > 0) {
+            if (!(ok = wait_tiles(done, max(0, c - dt), min(nt - 1, c + dt), base + i, st,
+                                  P.timeout_ns, 4)))
+              break;
+          }
+          const int p_hi = min(P.npairs, (c + 1) * tp);
+          if (i == 0) {
+            for (int p = c * tp + threadIdx.x; p < p_hi; p += blockDim.x) stage_first(p);
+          } else if (i < s - 1) {
+            for (int p = c * tp + threadIdx.x; p < p_hi; p += blockDim.x) stage_mid(i, p);
+          } else {
+            for (int p = c * tp + threadIdx.x; p < p_hi; p += blockDim.x) stage_last(p);
+          }
+          publish_tile(done, c, base + i + 1);
+        }
+        __syncthreads();
+        tk = s_tk[slot ^ 1];
+        slot ^= 1;
+      }
+      if (!ok) break;
+    } else {
+      for (int p = p0; p < pend; p += pstep) stage_first(p);
+      if (!(ok = stage_sync(P, c_lo, c_hi, ++progress, 1))) break;
+      for (int i = 1; i < s - 1; ++i) {
+        for (int p = p0; p < pend; p += pstep) stage_mid(i, p);
+        if (!(ok = stage_sync(P, c_lo, c_hi, ++progress, 2))) break;
+      }
+      if (!ok) break;
+      for (int p = p0; p < pend; p += pstep) stage_last(p);
     }
     double emax = em.best;
 #pragma unroll
@@ -283,9 +327,19 @@ static cudaError_t launch_one(const PlainParams &p, int blocks_per_sm, int num_s
   if (grid > kMaxPlainGrid) grid = kMaxPlainGrid;
   PlainParams q = p;
   q.nblocks = grid + (p.extra_arrivals > 0 ? p.extra_arrivals : 0);
+  size_t words = grid;
+  if (p.schedule == kScheduleFlow) {
+    // skew K: by default about one ticket window of the grid, so that a tile's
+    // dependencies were handed out a full round of CTAs earlier
+    int K = p.flow_skew > 0 ? p.flow_skew : (grid + p.s - 1) / p.s;
+    if (K < p.flow_dep) K = p.flow_dep;
+    if (K < 1) K = 1;
+    q.flow_skew = K;
+    words = flow_words(p.flow_ntiles);
+  }
   void *args[] = {&q};
   *grid_out = grid;
-  e = cudaMemsetAsync(p.flags, 0, sizeof(unsigned int) * grid, stream);
+  e = cudaMemsetAsync(p.flags, 0, sizeof(unsigned int) * words, stream);
   if (e != cudaSuccess) return e;
   return cudaLaunchCooperativeKernel((const void *)kern, dim3(grid), dim3(kThreads), args, 0,
                                      stream);

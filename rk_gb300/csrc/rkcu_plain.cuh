@@ -27,8 +27,13 @@ struct PlainParams {
   double2 *w[kMaxStages];             // w[1..s-1]
   double2 *dy, *err;
   DevState *st;
-  unsigned int *flags;                // kMaxPlainGrid progress words (reset by each launch)
-  int schedule;                       // kScheduleGrid or kScheduleNeighbour
+  unsigned int *flags;                // progress words (reset by each launch): kMaxPlainGrid
+                                      // CTA words, or the flow schedule's 2 tickets + tiles
+  int schedule;                       // kScheduleGrid, kScheduleNeighbour or kScheduleFlow
+  int flow_tile;                      // flow schedule: pairs per tile
+  int flow_ntiles;                    //   tiles per stage
+  int flow_dep;                       //   tiles either side a stage's stencil reads
+  int flow_skew;                      //   K: stage i runs K tiles behind stage i-1
   // per-step trace (include/tools.h:239-256, -DDUMP): for attempted step k <
   // trace_cap, trace_meta[3k..3k+2] = t, h, error max and, if trace_y is set,
   // trace_y[k * npairs ..] = the step's candidate state
@@ -43,9 +48,14 @@ struct PlainParams {
 // Largest grid the plain kernel uses (the progress words are sized for it).
 constexpr int kMaxPlainGrid = 2048;
 // Stage synchronisation of the plain kernel: a grid barrier after every stage
-// (grid-stride work), or per-CTA ranges with neighbour progress flags.
+// (grid-stride work), per-CTA ranges with neighbour progress flags, or a
+// dataflow over (stage, tile) tickets in wavefront order (one grid barrier per
+// step; the window of live rows stays in L2).
 constexpr int kScheduleGrid = 1;
 constexpr int kScheduleNeighbour = 2;
+constexpr int kScheduleFlow = 3;
+// Progress words the flow schedule needs for ntiles tiles.
+inline size_t flow_words(int ntiles) { return 2 + static_cast<size_t>(ntiles); }
 
 // Launches one persistent kernel (cooperative) for up to p.budget steps.
 // mode: kArithFused, kArithExact or kArithExactSoftMul
