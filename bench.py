@@ -51,6 +51,19 @@ FP64_GOPS_MEASURED = 505.0
 FP64_PER_SM_CLK = 2.0
 
 
+# DRAM bytes per component-step of the step-loop kernel, measured with ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum) at N=2000, DOPRI5(4); all
+# vectors exceed L2 at that size and above, so the figure scales with n.
+MEASURED_TRAFFIC = {
+    ("d", "exact", "DOPRI54"): (480.0, "one-pass ncu capture of the timed launches of this benchmark at N=2000"),
+    ("d", "mixed", "DOPRI54"): (327.0, "ncu --set full of a 3-step launch at N=2000, scaled by n"),
+}
+
+KERNEL_NAME = {"d": "plain_kernel (persistent, all stages of K steps)",
+               "lowstorage": "ls_kernel (persistent wavefront, K steps)",
+               "mixed": "mixed_kernel (persistent, all stages of K steps)"}
+
+
 def fp64_ops_per_comp(method, precision):
     """(FP64-pipe instructions, FP64 operations) per component-step of the
     BRUSS2D-MIX step loop, counted from the kernel.  Operations: a right-hand
@@ -312,6 +325,9 @@ def run_ours(args):
     nsm = torch.cuda.get_device_properties(local).multi_processor_count
     clk_mhz = clk.get("sm_mhz") or 2070.0
     fp64_peak = FP64_PER_SM_CLK * nsm * clk_mhz * 1e6 / 1e9
+    tr = MEASURED_TRAFFIC.get((args.variant, args.precision, args.method))
+    traffic = tr[0] * n * steps_done / max(1, launches) if tr else None
+    kname = KERNEL_NAME["mixed" if args.precision == "mixed" else args.variant]
     line = {
         "metric": f"BRUSS2D-MIX N={args.grid} {args.method} steps/s", "value": value, "unit": "steps/s",
         "n_gpus": ws, "steps": steps_done, "warmup": args.warmup,
@@ -324,8 +340,10 @@ def run_ours(args):
                    "precision": args.precision, "variant": args.variant, "parallelism": f"replicas{ws}",
                    "l2": f"per-step working set {dev_bytes / 1e6:.0f} MB > {L2_BYTES / 1e6:.0f} MB L2, no flush"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "peak_kind": peak_kind,
-                     "kernel": "plain_kernel (persistent, all stages of K steps)"},
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "traffic_bytes_per_component_step": tr[0] if tr else None,
+                     "traffic_source": tr[1] if tr else "not measured for this configuration",
+                     "kernel": kname},
         "fp64_roofline": {"achieved": fp64_achieved, "peak": fp64_peak,
                           "unit": "G FP64 instr/s", "frac": fp64_achieved / fp64_peak,
                           "peak_kind": f"2 FP64 instr/clk/SM x {nsm} SMs at the sampled {clk_mhz:.0f} MHz "
