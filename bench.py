@@ -492,14 +492,14 @@ def run_served(args):
 
     reqs = workloads.served_requests(20000, seed=7)[: args.requests]
     # capacity estimate: component-steps of the sample at the batched rate measured
-    # on this part (3.2e9 component-steps/s in FP64 exact mode)
+    # on this part (4.7e9 component-steps/s in the FP64 exact mode, 1024 instances)
     work = 0.0
     for r in reqs:
         if r["kind"] == "bruss":
             work += workloads.estimated_work(dict(grid_n=r["grid_n"], alpha=2e-3))
         else:
             work += r["n"] * 40.0
-    busy = work / (3.2e9 if args.precision == "exact" else 4.8e9)
+    busy = work / 4.7e9
     span = reqs[-1]["arrival"]
     scale = busy / (args.load * span)
     loop = serving.ServingLoop(int(args.arena_gb * (1 << 30)), max_instances=4096,
@@ -524,8 +524,8 @@ def run_served(args):
         "latency_s": {"p50": out["p50"], "p99": out["p99"], "max": float(np.max(out["latency"]))},
         "admission_refusals": out["refusals"], "makespan_s": out["makespan"], "clocks": clk,
     }
-    if args.plain_requests > 0:
-        sub = reqs[: args.plain_requests]
+    if args.plain_requests != 0:
+        sub = reqs if args.plain_requests < 0 else reqs[: args.plain_requests]
         pl = serving.serve_plain(sub, time_scale=scale, precision=args.precision)
         line["plain_form"] = {"value": pl["solves_per_s"], "unit": "solves/s",
                               "p50": pl["p50"], "p99": pl["p99"],
@@ -547,7 +547,8 @@ def main():
     ap.add_argument("--requests", type=int, default=400)
     ap.add_argument("--load", type=float, default=0.5)
     ap.add_argument("--arena-gb", type=float, default=8.0)
-    ap.add_argument("--plain-requests", type=int, default=100)
+    ap.add_argument("--plain-requests", type=int, default=-1,
+                    help="served: requests the plain form serves for comparison (-1: all)")
     ap.add_argument("--instances", type=int, default=1024)
     ap.add_argument("--sweeps-per-launch", type=int, default=256)
     ap.add_argument("--plain-sample", type=int, default=32)
