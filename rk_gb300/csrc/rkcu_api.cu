@@ -74,7 +74,7 @@ struct rkcu_solver {
   double2 *y[2] = {nullptr, nullptr};
   double2 *stage = nullptr;  // w[1..s-1], dy, err
   int stage_vectors = 0;
-  float2 *mstage = nullptr;  // mixed form: f0, y32, S[2..s-1], dys, dyc, err
+  float2 *mstage = nullptr;  // mixed form: f0, y32, dF[1..s-2]
   int mstage_vectors = 0;
   double2 *rings = nullptr;  // low-storage form: ring buffers
   size_t ring_pairs = 0;
@@ -292,7 +292,7 @@ int rkcu_begin(rkcu_solver *s, double t0, double te, const double *y0, int y0_on
   if (tol <= 0.0 && s->opt.step_limit <= 0) return RKCU_ERR_INVALID;  // fixed step needs a limit
   RKCU_CK(cudaSetDevice(s->opt.device));
   if (s->opt.precision == RKCU_MIXED) {
-    const int mneed = s->s + 3;  // f0, y32, S[2..s-1], dys, dyc, err
+    const int mneed = s->s;  // f0, y32, dF[1..s-2]
     if (s->mstage_vectors < mneed) {
       if (s->mstage) {
         RKCU_CK(cudaStreamSynchronize(s->stream));
@@ -451,15 +451,13 @@ int rkcu_advance(rkcu_solver *s, int max_steps) {
     const size_t np = s->npairs;
     m.f0 = s->mstage;
     m.y32 = s->mstage + np;
-    for (int l = 2; l < s->s; ++l) m.S[l] = s->mstage + (size_t)l * np;
-    m.dys = s->mstage + (size_t)s->s * np;
-    m.dyc = s->mstage + (size_t)(s->s + 1) * np;
-    m.err = s->mstage + (size_t)(s->s + 2) * np;
+    for (int j = 1; j <= s->s - 2; ++j) m.dF[j] = s->mstage + (size_t)(1 + j) * np;
     m.st = s->st;
     m.bruss.N = s->prob.grid_n;
     m.bruss.coef = bruss_coef(&s->prob);
     int grid = 0;
-    cudaError_t e = rkcu::launch_mixed(m, s->num_sms, s->stream, &grid);
+    // schedule 1 keeps the plain loads (the TMA path needs even N, s <= 8)
+    cudaError_t e = rkcu::launch_mixed(m, s->opt.schedule != 1, s->num_sms, s->stream, &grid);
     if (e != cudaSuccess) return cuda_fail(e, "mixed kernel launch");
     s->last_grid = grid;
     ++s->launches;

@@ -1,28 +1,50 @@
-// Mixed-precision form of the step loop (BRUSS2D-MIX): FP32 stage vectors and
-// right-hand-side increments, FP64 state, FP64 update and error-norm reduction.
+// Mixed-precision form of the step loop (BRUSS2D-MIX): FP32 stage increments,
+// FP64 state, FP64 update and error-norm reduction.
 //
 // On GB300 the FP64 pipe (and every FP64<->FP32 conversion) runs at 1/72 of
 // the FP32 rate, so the FP32 stages must avoid both.  Per step and component:
 //   F0 = f(y)                          FP64 (fused), once per step
 //   y1 = y + (h * sum b) * F0           FP64, the large part of the update
-//   stage i >= 1:  delta_i = h c_i F0 + S_i,  S_i = sum_{1<=j<i} h a_ij dF_j   (FP32)
+//   stage i >= 1:  delta_i = h c_i F0 + sum_{1<=j<i} h a_ij dF_j                (FP32)
 //                  dF_i = f(y + delta_i) - F0 = alpha (N-1)^2 lap(delta_i)
 //                         + [u^2 v](y + delta) - [u^2 v](y) -/+ 4.4 du / 3.4 du  (FP32)
 //     (the Laplacian is linear, and the cubic term is expanded exactly, so the
 //      large diffusion coefficient never multiplies FP32 rounding of y itself)
-//   dY = sum_{j>=1} h b_j dF_j          FP32, Kahan-compensated across stages
+//   dY = sum_{j>=1} h b_j dF_j          FP32, Kahan-compensated, in order of j
 //   e  = sum_{j>=1} h (b_j - b^_j) dF_j FP32 (the F0 terms cancel: sum(b - b^) = 0)
 //   y_new = y1 + dY                     FP64
 //   err max = max |e| / max(|y_new|, |y_old|): per thread in FP32, reduced in FP64
 // c_i is taken as the row sum of A (sum_j a_ij), so sum_j h a_ij F0 = h c_i F0.
 // FP64 instructions per component-step: about 12 (RHS 7.5, update 2, two
 // conversions) instead of 85-128 for the FP64 forms.
+//
+// Memory: this form is bound by HBM traffic, not arithmetic, so it stores each
+// stage's dF_i once and gathers delta_i from dF_1 .. dF_{i-1} at the five
+// stencil points when stage i runs (FP32 multiply-adds are cheap here, and the
+// neighbours' reads hit L1/L2), instead of scattering dF_i into running sums
+// that every later stage reads and rewrites (the D order of the FP64 forms).
+// dY and e are formed in the last stage from the stored dF_j.  DRAM traffic
+// per grid point and step: about 336 bytes instead of 656, in s FP32 vectors
+// (f0, y32, dF_1 .. dF_{s-2}) instead of s + 3.
+#include <cudaTypedefs.h>  // PFN_cuTensorMapEncodeTiled
+
 #include "rkcu.h"
 #include "rkcu_mixed.cuh"
+#include "rkcu_tma.cuh"
 
 namespace rkcu {
 
 constexpr int kMixThreads = 256;
+// FP32 stages work on tiles of kTileR x kTileC grid points (one warp per tile
+// row), so delta_i is gathered once per point of the tile and its halo
+constexpr int kTileR = 8, kTileC = 32;
+static_assert(kTileR * kTileC == kMixThreads, "one grid point per thread");
+// TMA box per vector: kTileR + 2 rows of kBoxPairs pairs starting two columns
+// left of the tile (the box must start at an even pair: 16-byte rule), i.e.
+// the tile, its one-point halo and one spare column either side.
+constexpr int kBoxRows = kTileR + 2, kBoxPairs = kTileC + 4;
+constexpr unsigned kBoxBytes = kBoxRows * kBoxPairs * 8;
+constexpr unsigned kSlotBytes = (kBoxBytes + 127) / 128 * 128;  // 128-byte aligned slots
 
 // float with the sign, exponent and leading 23 mantissa bits of x (truncation),
 // built with integer instructions: a double->float conversion runs on the FP64
@@ -37,43 +59,21 @@ __device__ __forceinline__ float trunc_to_float(double x) {
   return __uint_as_float(bits);
 }
 
-// delta_i at pair q: h c_i F0(q) + S_i(q)
-struct DeltaView {
-  const float2 *__restrict__ f0;
-  const float2 *__restrict__ S;  // null for stage 1
-  float hc;
-  __device__ __forceinline__ float2 at(int q) const {
-    const float2 f = f0[q];
-    float2 d = make_float2(hc * f.x, hc * f.y);
-    if (S) {
-      const float2 s = S[q];
-      d.x += s.x;
-      d.y += s.y;
-    }
-    return d;
-  }
-};
-
-// dF_i at grid point p (both components)
-__device__ __forceinline__ float2 delta_rhs(const DeltaView &dv, const float2 y32, int p, int N,
-                                            float coef) {
-  const int k = p / N;
-  const int j = p - k * N;
-  const float2 c = dv.at(p);
-  const float2 up = dv.at(k == 0 ? p + N : p - N);
-  const float2 dn = dv.at(k == N - 1 ? p - N : p + N);
+// dF_i at one grid point from delta_i at the point (c), its vertical
+// neighbours (up, dn: the row above/below, or the inner row twice at a
+// boundary row) and horizontal ones; jcase 1: first column (only e, doubled),
+// 2: last column (only w, doubled), 0: interior.
+__device__ __forceinline__ float2 delta_rhs(const float2 c, const float2 up, const float2 dn,
+                                            const float2 w, const float2 e, int jcase,
+                                            const float2 y32, float coef) {
   float lu = up.x + dn.x, lv = up.y + dn.y;
-  if (j == 0) {
-    const float2 e = dv.at(p + 1);
+  if (jcase == 1) {
     lu = fmaf(2.0f, e.x, lu);
     lv = fmaf(2.0f, e.y, lv);
-  } else if (j == N - 1) {
-    const float2 w = dv.at(p - 1);
+  } else if (jcase == 2) {
     lu = fmaf(2.0f, w.x, lu);
     lv = fmaf(2.0f, w.y, lv);
   } else {
-    const float2 w = dv.at(p - 1);
-    const float2 e = dv.at(p + 1);
     lu = (lu + w.x) + e.x;
     lv = (lv + w.y) + e.y;
   }
@@ -85,14 +85,52 @@ __device__ __forceinline__ float2 delta_rhs(const DeltaView &dv, const float2 y3
   return make_float2(fmaf(coef, lu, fmaf(-4.4f, du, dX)), fmaf(coef, lv, fmaf(3.4f, du, -dX)));
 }
 
-__global__ void __launch_bounds__(kMixThreads) mixed_kernel(const __grid_constant__ MixedParams P) {
+// delta_i at pair q: h c_i F0(q) + sum over the stage's nonzero j of h a_ij dF_j(q),
+// accumulated in order of j (jp: the dF_j vectors, ja: h a_ij, nj of them, at most
+// kMaxJ).  All loads are issued before the multiply-adds that use them.
+template <int kMaxJ>
+__device__ __forceinline__ float2 delta_at(const float2 *const *jp, const float *ja, int nj,
+                                           const float2 *__restrict__ f0, float hc, int q) {
+  float2 d[kMaxJ > 0 ? kMaxJ : 1];
+#pragma unroll
+  for (int k = 0; k < kMaxJ; ++k)
+    if (k < nj) d[k] = jp[k][q];
+  const float2 f = f0[q];
+  float2 acc = make_float2(0.0f, 0.0f);
+#pragma unroll
+  for (int k = 0; k < kMaxJ; ++k) {
+    if (k < nj) {
+      acc.x = fmaf(ja[k], d[k].x, acc.x);
+      acc.y = fmaf(ja[k], d[k].y, acc.y);
+    }
+  }
+  return make_float2(fmaf(hc, f.x, acc.x), fmaf(hc, f.y, acc.y));
+}
+
+// kMaxS: an upper bound of the stage count (8 or 13), so that the per-stage
+// loops over earlier stages unroll.
+template <int kMaxS>
+__global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
+    mixed_kernel(const __grid_constant__ MixedParams P) {
+  // TMA staging buffers: 2 (double buffer) x s slots of kSlotBytes, from the
+  // first 128-byte boundary of the dynamic shared memory (128 bytes spare)
+  extern __shared__ __align__(128) unsigned char s_dyn[];
+  unsigned char *const s_box = s_dyn + ((128u - (smem_u32(s_dyn) & 127u)) & 127u);
+  __shared__ __align__(8) uint64_t s_mbar[2];
   __shared__ double s_t, s_h;
   __shared__ int s_acc, s_rej, s_cur, s_done;
   __shared__ unsigned long long s_step;
   __shared__ double s_wmax[kMixThreads / 32];
-  __shared__ float hA[kMaxStages * kMaxStages], hb[kMaxStages], hbh[kMaxStages], hc[kMaxStages];
+  __shared__ float hb[kMaxStages], hbh[kMaxStages], hc[kMaxStages];
+  // per stage i: the j < i with a_ij != 0 (j = 1 always, as the running sums
+  // of the scatter order start there) and h a_ij, for the gather
+  __shared__ const float2 *s_jp[kMaxStages][kMaxStages];
+  __shared__ int s_jl[kMaxStages][kMaxStages];
+  __shared__ float s_ja[kMaxStages][kMaxStages];
+  __shared__ int s_nj[kMaxStages];
   __shared__ double s_hbsum;
   __shared__ float s_hbhsum;
+  __shared__ float2 s_delta[kTileR + 2][kTileC + 2];  // delta_i on a tile and its halo
 
   DevState *st = P.st;
   const int s = P.s;
@@ -111,14 +149,31 @@ __global__ void __launch_bounds__(kMixThreads) mixed_kernel(const __grid_constan
     s_done = st->done;
     s_step = st->step;
   }
+  if (threadIdx.x == 0 && P.use_tma) {
+    mbar_init(&s_mbar[0], 1);
+    mbar_init(&s_mbar[1], 1);
+    mbar_fence_init();
+  }
   __syncthreads();
+  unsigned phase = 0;    // parity of the next completion of each TMA buffer (bits 0, 1)
+  unsigned pending = 0;  // buffers with copies issued and not yet waited for (bits 0, 1)
 
   bool ok = true;
   for (int it = 0; it < P.budget; ++it) {
     if (s_done) break;
     const double h = s_h;
-    for (int idx = threadIdx.x; idx < kMaxStages * kMaxStages; idx += blockDim.x)
-      hA[idx] = static_cast<float>(h * P.A[idx]);
+    if (threadIdx.x < kMaxStages) {
+      const int i = threadIdx.x;
+      int nj = 0;
+      for (int j = 1; j < i && i < s; ++j) {
+        if (j > 1 && !P.nzA[i * kMaxStages + j]) continue;
+        s_jp[i][nj] = P.dF[j];
+        s_jl[i][nj] = j;
+        s_ja[i][nj] = static_cast<float>(h * P.A[i * kMaxStages + j]);
+        ++nj;
+      }
+      s_nj[i] = nj;
+    }
     if (threadIdx.x < kMaxStages) {
       hb[threadIdx.x] = static_cast<float>(h * P.b[threadIdx.x]);
       hbh[threadIdx.x] = static_cast<float>(h * P.bh[threadIdx.x]);
@@ -143,60 +198,151 @@ __global__ void __launch_bounds__(kMixThreads) mixed_kernel(const __grid_constan
         P.y32[p] = make_float2(trunc_to_float(Y.x), trunc_to_float(Y.y));
       }
     }
+    if (P.use_tma) fence_proxy_async_global();  // f0, y32 are read by TMA next
     if (!(ok = grid_barrier(st, P.nblocks, P.timeout_ns, 11))) break;
 
     float emax = 0.0f;
+    const int N = br.N;
+    const int tiles_x = (N + kTileC - 1) / kTileC;
+    const int ntiles = tiles_x * ((N + kTileR - 1) / kTileR);
+    const int tr = threadIdx.x / kTileC, tc = threadIdx.x % kTileC;
     for (int i = 1; i < s; ++i) {
-      DeltaView dv{P.f0, i >= 2 ? P.S[i] : nullptr, hc[i]};
       const bool last = (i == s - 1);
-      const float bi = hb[i], bhi = hbh[i];
-      for (int p = gtid; p < P.npairs; p += gstride) {
-        const float2 y32 = P.y32[p];
-        const float2 dF = delta_rhs(dv, y32, p, br.N, coef);
-        for (int l = i + 1; l < s; ++l) {
-          if (!P.nzA[l * kMaxStages + i] && i > 1) continue;
-          const float a = hA[l * kMaxStages + i];
-          float2 acc = (i == 1) ? make_float2(0.f, 0.f) : P.S[l][p];
-          acc.x = fmaf(a, dF.x, acc.x);
-          acc.y = fmaf(a, dF.y, acc.y);
-          P.S[l][p] = acc;
+      const float2 *const *jp = s_jp[i];
+      const float *ja = s_ja[i];
+      const int nj = s_nj[i];
+      const float hci = hc[i];
+      // dF_i (and, in the last stage, dY, e and y_new) at grid point p from
+      // delta_i on the tile (s_delta), y32, and the point's own dF_j / f0
+      auto finish_point = [&](int tr_, int tc_, int k, int j, float2 y32, auto &&own_dF,
+                              auto &&own_f0) {
+        const int p = k * N + j;
+        const int jcase = j == 0 ? 1 : (j == N - 1 ? 2 : 0);
+        const float2 c = s_delta[tr_ + 1][tc_ + 1];
+        const float2 up = s_delta[k == 0 ? tr_ + 2 : tr_][tc_ + 1];
+        const float2 dn = s_delta[k == N - 1 ? tr_ : tr_ + 2][tc_ + 1];
+        const float2 w = s_delta[tr_ + 1][tc_];
+        const float2 e = s_delta[tr_ + 1][tc_ + 2];
+        const float2 dF = delta_rhs(c, up, dn, w, e, jcase, y32, coef);
+        if (!last) {
+          P.dF[i][p] = dF;
+          return;
         }
-        // Kahan-compensated dY and the error estimate
-        float2 sum, cmp, e;
-        if (i == 1) {
-          // the F0 terms of the error estimate: h sum(b - b^) F0 (zero for embedded pairs)
-          const float2 f = P.f0[p];
-          sum = make_float2(0.f, 0.f);
-          cmp = make_float2(0.f, 0.f);
-          e = make_float2(s_hbhsum * f.x, s_hbhsum * f.y);
-        } else {
-          sum = P.dys[p];
-          cmp = P.dyc[p];
-          e = P.err[p];
-        }
-        {
-          const float ax = fmaf(bi, dF.x, -cmp.x), ay = fmaf(bi, dF.y, -cmp.y);
+        // dY (Kahan-compensated) and the error estimate, in order of the stages
+        const float2 f = own_f0();
+        float2 sum = make_float2(0.f, 0.f), cmp = make_float2(0.f, 0.f);
+        float2 er = make_float2(s_hbhsum * f.x, s_hbhsum * f.y);
+        float2 dj[kMaxS - 1];
+#pragma unroll
+        for (int jj = 1; jj < kMaxS - 1; ++jj)
+          if (jj < s - 1) dj[jj] = own_dF(jj);
+#pragma unroll
+        for (int jj = 1; jj < kMaxS; ++jj) {
+          if (jj >= s) break;
+          const float2 d = jj == s - 1 ? dF : dj[jj < kMaxS - 1 ? jj : 0];
+          const float ax = fmaf(hb[jj], d.x, -cmp.x), ay = fmaf(hb[jj], d.y, -cmp.y);
           const float tx = sum.x + ax, ty = sum.y + ay;
           cmp.x = (tx - sum.x) - ax;
           cmp.y = (ty - sum.y) - ay;
           sum.x = tx;
           sum.y = ty;
+          er.x = fmaf(hbh[jj], d.x, er.x);
+          er.y = fmaf(hbh[jj], d.y, er.y);
         }
-        e.x = fmaf(bhi, dF.x, e.x);
-        e.y = fmaf(bhi, dF.y, e.y);
-        if (!last) {
-          P.dys[p] = sum;
-          P.dyc[p] = cmp;
-          P.err[p] = e;
-        } else {
-          const double2 y1 = ynew[p];
-          const double2 yn = make_double2(y1.x + static_cast<double>(sum.x - cmp.x),
-                                          y1.y + static_cast<double>(sum.y - cmp.y));
-          ynew[p] = yn;
-          const float dnx = fmaxf(fabsf(trunc_to_float(yn.x)), fabsf(y32.x));
-          const float dny = fmaxf(fabsf(trunc_to_float(yn.y)), fabsf(y32.y));
-          emax = fmaxf(emax, dnx == 0.0f ? 3.0e38f : fabsf(e.x) / dnx);
-          if (2 * p + 1 < P.n) emax = fmaxf(emax, dny == 0.0f ? 3.0e38f : fabsf(e.y) / dny);
+        const double2 y1 = ynew[p];
+        const double2 yn = make_double2(y1.x + static_cast<double>(sum.x - cmp.x),
+                                        y1.y + static_cast<double>(sum.y - cmp.y));
+        ynew[p] = yn;
+        const float dnx = fmaxf(fabsf(trunc_to_float(yn.x)), fabsf(y32.x));
+        const float dny = fmaxf(fabsf(trunc_to_float(yn.y)), fabsf(y32.y));
+        emax = fmaxf(emax, dnx == 0.0f ? 3.0e38f : fabsf(er.x) / dnx);
+        if (2 * p + 1 < P.n) emax = fmaxf(emax, dny == 0.0f ? 3.0e38f : fabsf(er.y) / dny);
+      };
+
+      if (P.use_tma) {
+        // Tiles through TMA, double-buffered: while tile t is evaluated, the
+        // boxes of the CTA's next tile are in flight.  Box slot 0: f0, 1: y32,
+        // 1 + j: dF_j for j < i.
+        const int nvec = 1 + i;
+        const unsigned tile_bytes = nvec * kBoxBytes;
+        auto slot = [&](int b, int v) {
+          return reinterpret_cast<const float2 *>(s_box + (static_cast<size_t>(b) * s + v) * kSlotBytes);
+        };
+        auto issue = [&](int t, int b) {
+          const int k0 = (t / tiles_x) * kTileR, j0 = (t % tiles_x) * kTileC;
+          mbar_arrive_expect_tx(&s_mbar[b], tile_bytes);
+          for (int v = 0; v < nvec; ++v)
+            tma_load_2d(s_box + (static_cast<size_t>(b) * s + v) * kSlotBytes, &P.tm[v],
+                        2 * (j0 - 2), k0 - 1, &s_mbar[b]);
+        };
+        int b = 0;
+        __syncthreads();  // the buffers are free (the previous stage is done with them)
+        if (blockIdx.x < ntiles) {
+          if (threadIdx.x == 0) issue(blockIdx.x, 0);
+          pending |= 1u;
+        }
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, b ^= 1) {
+          const int tn = t + gridDim.x;
+          __syncthreads();  // buffer b^1 and s_delta are free
+          if (tn < ntiles) {
+            if (threadIdx.x == 0) issue(tn, b ^ 1);
+            pending |= 2u >> b;  // bit of buffer b^1
+          }
+          const bool got = mbar_wait(&s_mbar[b], (phase >> b) & 1u, st, P.timeout_ns, 14);
+          if (!__syncthreads_and(got)) {
+            ok = false;
+            break;
+          }
+          phase ^= 1u << b;
+          pending &= ~(1u << b);
+          const int k0 = (t / tiles_x) * kTileR, j0 = (t % tiles_x) * kTileC;
+          const float2 *bf0 = slot(b, 0);
+          for (int hh = threadIdx.x; hh < (kTileR + 2) * (kTileC + 2); hh += blockDim.x) {
+            const int hr = hh / (kTileC + 2), hcl = hh % (kTileC + 2);
+            const int k = k0 + hr - 1, j = j0 + hcl - 1;
+            if (k < 0 || k >= N || j < 0 || j >= N) continue;
+            const int e = hr * kBoxPairs + hcl + 1;
+            float2 acc = make_float2(0.0f, 0.0f);
+#pragma unroll
+            for (int kk = 0; kk < kMaxS - 2; ++kk) {
+              if (kk < nj) {
+                const float2 d = slot(b, 1 + s_jl[i][kk])[e];
+                acc.x = fmaf(ja[kk], d.x, acc.x);
+                acc.y = fmaf(ja[kk], d.y, acc.y);
+              }
+            }
+            const float2 f = bf0[e];
+            s_delta[hr][hcl] = make_float2(fmaf(hci, f.x, acc.x), fmaf(hci, f.y, acc.y));
+          }
+          __syncthreads();
+          const int k = k0 + tr, j = j0 + tc;
+          if (k < N && j < N) {
+            const int eo = (tr + 1) * kBoxPairs + tc + 2;  // the point itself in a box
+            finish_point(tr, tc, k, j, slot(b, 1)[eo],
+                         [&](int jj) { return slot(b, 1 + jj)[eo]; },
+                         [&]() { return bf0[eo]; });
+          }
+        }
+        if (!ok) break;
+        fence_proxy_async_global();  // dF_i is read by TMA in later stages
+      } else {
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+          // delta_i on the tile and a one-point halo (rows and columns outside
+          // the grid are not needed: a boundary uses the inner neighbour twice)
+          const int k0 = (t / tiles_x) * kTileR, j0 = (t % tiles_x) * kTileC;
+          __syncthreads();  // the previous tile's reads of s_delta are done
+          for (int hh = threadIdx.x; hh < (kTileR + 2) * (kTileC + 2); hh += blockDim.x) {
+            const int hr = hh / (kTileC + 2), hcl = hh % (kTileC + 2);
+            const int k = k0 + hr - 1, j = j0 + hcl - 1;
+            if (k >= 0 && k < N && j >= 0 && j < N)
+              s_delta[hr][hcl] = delta_at<kMaxS - 2>(jp, ja, nj, P.f0, hci, k * N + j);
+          }
+          __syncthreads();
+          const int k = k0 + tr, j = j0 + tc;
+          if (k >= N || j >= N) continue;
+          const int p = k * N + j;
+          finish_point(tr, tc, k, j, P.y32[p], [&](int jj) { return P.dF[jj][p]; },
+                       [&]() { return P.f0[p]; });
         }
       }
       if (!last) {
@@ -245,6 +391,13 @@ __global__ void __launch_bounds__(kMixThreads) mixed_kernel(const __grid_constan
     __syncthreads();
   }
 
+  // after a failed wait, let the copies still in flight land before the CTA
+  // leaves (bounded as well)
+  if (pending && threadIdx.x == 0) {
+    for (int b = 0; b < 2; ++b)
+      if ((pending >> b) & 1u) mbar_wait(&s_mbar[b], (phase >> b) & 1u, st, P.timeout_ns, 15);
+  }
+
   if (ok && blockIdx.x == 0 && threadIdx.x == 0) {
     st->t = s_t;
     st->h = s_h;
@@ -257,20 +410,62 @@ __global__ void __launch_bounds__(kMixThreads) mixed_kernel(const __grid_constan
   }
 }
 
-cudaError_t launch_mixed(const MixedParams &p, int num_sms, cudaStream_t stream, int *grid_out) {
+// cuTensorMapEncodeTiled from the driver, found once through the runtime
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+
+// 2-D map of an N x N grid of float2 pairs (rows of 2N floats) with boxes of
+// kBoxRows rows x kBoxPairs pairs; false if the layout does not allow TMA.
+static bool encode_box_map(CUtensorMap *m, const float2 *base, int N) {
+  auto fn = encode_fn();
+  if (!fn || N % 2 || (reinterpret_cast<uintptr_t>(base) & 15)) return false;
+  const cuuint64_t dims[2] = {2ull * N, static_cast<cuuint64_t>(N)};
+  const cuuint64_t strides[1] = {8ull * N};  // bytes between rows: a multiple of 16 for even N
+  const cuuint32_t box[2] = {2u * kBoxPairs, static_cast<cuuint32_t>(kBoxRows)};
+  const cuuint32_t estr[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float2 *>(base), dims, strides, box, estr,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+cudaError_t launch_mixed(const MixedParams &p, bool tma, int num_sms, cudaStream_t stream,
+                         int *grid_out) {
+  MixedParams q = p;
+  q.use_tma = 0;
+  if (tma && p.s <= kMixTmaStages) {
+    bool good = encode_box_map(&q.tm[0], p.f0, p.bruss.N) && encode_box_map(&q.tm[1], p.y32, p.bruss.N);
+    for (int j = 1; good && j <= p.s - 2; ++j) good = encode_box_map(&q.tm[1 + j], p.dF[j], p.bruss.N);
+    q.use_tma = good ? 1 : 0;
+  }
+  const void *kern = p.s <= 8 ? (const void *)mixed_kernel<8> : (const void *)mixed_kernel<kMaxStages>;
+  const size_t dyn = q.use_tma ? 2ull * p.s * kSlotBytes + 128 : 0;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+  if (e != cudaSuccess) return e;
   int occ = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, mixed_kernel, kMixThreads, 0);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kMixThreads, dyn);
   if (e != cudaSuccess) return e;
   if (occ < 1) return cudaErrorInvalidConfiguration;
   int grid = occ * num_sms;
   const int useful = (p.npairs + kMixThreads - 1) / kMixThreads;
   if (grid > useful) grid = useful > 0 ? useful : 1;
-  MixedParams q = p;
   q.nblocks = grid + (p.extra_arrivals > 0 ? p.extra_arrivals : 0);
   void *args[] = {&q};
   *grid_out = grid;
-  return cudaLaunchCooperativeKernel((const void *)mixed_kernel, dim3(grid), dim3(kMixThreads), args,
-                                     0, stream);
+  return cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(kMixThreads), args, dyn, stream);
 }
 
 }  // namespace rkcu

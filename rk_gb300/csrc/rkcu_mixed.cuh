@@ -1,9 +1,15 @@
 // Mixed-precision step loop (FP32 stage vectors, FP64 state and norm), BRUSS2D-MIX.
 #pragma once
 
+#include <cuda.h>  // CUtensorMap
+
 #include "rkcu_device.cuh"
 
 namespace rkcu {
+
+// TMA staging of the FP32 stages (even N, at most kMixTmaStages stages): one
+// tensor map per vector, slot 0 = f0, 1 = y32, 1 + j = dF_j.
+constexpr int kMixTmaStages = 8;
 
 struct MixedParams {
   int npairs, n, s, ord, step_limit, budget, nblocks, extra_arrivals;
@@ -14,11 +20,17 @@ struct MixedParams {
   double bsum, bhsum;                                       // sum b, sum (b - b^)
   unsigned char nzA[kMaxStages * kMaxStages];
   double2 *y[2];
-  float2 *f0, *y32, *S[kMaxStages], *dys, *dyc, *err;
+  float2 *f0, *y32;
+  float2 *dF[kMaxStages];  // dF[1 .. s-2]: the stages' right-hand-side increments
   DevState *st;
   Bruss bruss;
+  int use_tma;             // 1: stage tiles through TMA (tm valid), 0: plain loads
+  CUtensorMap tm[kMixTmaStages];
 };
 
-cudaError_t launch_mixed(const MixedParams &p, int num_sms, cudaStream_t stream, int *grid_out);
+// Launches the persistent mixed kernel; tma: stage tiles through TMA where the
+// grid allows it (even N, at most kMixTmaStages stages), else plain loads.
+cudaError_t launch_mixed(const MixedParams &p, bool tma, int num_sms, cudaStream_t stream,
+                         int *grid_out);
 
 }  // namespace rkcu

@@ -52,3 +52,33 @@ def test_mixed_rejects_problems_without_a_mixed_evaluator():
     with pytest.raises(rk.RkcuError) as ei:
         rk.Solver(rk.lv_pairs(100), precision="mixed")
     assert ei.value.status == rk.ERR_INVALID
+
+
+@pytest.mark.parametrize("N,method", [(64, "DOPRI54"), (250, "DOPRI54"), (48, "RKF23"),
+                                      (40, "DOPRI87")])
+def test_mixed_tma_staging_equals_plain_loads(N, method):
+    """The FP32 stages read their tiles either through TMA boxes staged in shared
+    memory (even N, at most 8 stages) or with plain loads (schedule 1); both
+    evaluate the same operations on the same values, so the bits agree."""
+    prob = rk.bruss2d_mix(N, 2e-3)
+    y0 = rk.ode_start(prob)
+    out = []
+    for sched in (0, 1):
+        with rk.Solver(prob, method=method, precision="mixed", schedule=sched) as s:
+            out.append(s.solve(0.0, 0.1, y0, 1e-6))
+    (a, sa), (b, sb) = out
+    assert (sa["steps_acc"], sa["steps_rej"]) == (sb["steps_acc"], sb["steps_rej"])
+    np.testing.assert_array_equal(a, b)
+
+
+def test_mixed_odd_grid_uses_plain_loads():
+    """An odd N cannot use TMA boxes (rows would not be 16-byte aligned); the
+    kernel falls back to plain loads and stays within the tolerance of FP64."""
+    N = 37
+    prob = rk.bruss2d_mix(N, 2e-3)
+    y0 = rk.ode_start(prob)
+    with rk.Solver(prob, method="DOPRI54", precision="exact") as s:
+        ref, _ = s.solve(0.0, 0.3, y0, 1e-6)
+    with rk.Solver(prob, method="DOPRI54", precision="mixed") as s:
+        y, _ = s.solve(0.0, 0.3, y0, 1e-6)
+    assert _rel(y, ref) <= 1e-6
