@@ -53,7 +53,7 @@ __device__ __forceinline__ float trunc_to_float(double x) {
   const int hi = __double2hiint(x);
   const unsigned lo = static_cast<unsigned>(__double2loint(x));
   const int e = ((hi >> 20) & 0x7ff) - 1023 + 127;
-  if (e <= 0 || e >= 255) return __double2float_rn(x);
+  if (e <= 0 || e >= 255) return softfp::hw_to_float(x);  // out of line: not if-converted
   const unsigned bits = (static_cast<unsigned>(hi) & 0x80000000u) | (static_cast<unsigned>(e) << 23) |
                         ((static_cast<unsigned>(hi) & 0xfffffu) << 3) | (lo >> 29);
   return __uint_as_float(bits);
@@ -194,7 +194,9 @@ __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
         const double2 F = br.eval<kArithFused>(ycur, p);
         const double2 Y = ycur[p];
         ynew[p] = make_double2(fma(hbs, F.x, Y.x), fma(hbs, F.y, Y.y));
-        P.f0[p] = make_float2(__double2float_rn(F.x), __double2float_rn(F.y));
+        // rounded to float on the integer pipe (the conversion instruction would
+        // use the FP64 pipe, this stage's bottleneck)
+        P.f0[p] = make_float2(softfp::to_float(F.x), softfp::to_float(F.y));
         P.y32[p] = make_float2(trunc_to_float(Y.x), trunc_to_float(Y.y));
       }
     }

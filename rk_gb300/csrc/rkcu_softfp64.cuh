@@ -85,6 +85,44 @@ inline double hw_add(double a, double b) {
 #endif
 }
 
+#ifdef __CUDACC__
+static __host__ __device__ __noinline__ float hw_to_float(double x) {
+#else
+inline float hw_to_float(double x) {
+#endif
+#ifdef __CUDA_ARCH__
+  return __double2float_rn(x);
+#else
+  return static_cast<float>(x);
+#endif
+}
+
+SFP_HD float float_of(uint32_t b) {
+#ifdef __CUDA_ARCH__
+  return __uint_as_float(b);
+#else
+  float x;
+  std::memcpy(&x, &b, 4);
+  return x;
+#endif
+}
+
+// x rounded to the nearest float, ties to even (a double -> float conversion
+// runs on the FP64 pipe on this part).  Results outside the normal float range
+// (and zeros, infinities, NaNs) come from the hardware conversion.
+SFP_HD float to_float(double x) {
+  const uint64_t bx = bits_of(x);
+  const uint32_t hi = static_cast<uint32_t>(bx >> 32);
+  const int e = static_cast<int>((hi >> 20) & 0x7ff) - 1023 + 127;  // float exponent field
+  if (e <= 0 || e >= 255) return hw_to_float(x);
+  const uint64_t m = bx & 0x000fffffffffffffull;
+  uint32_t r = static_cast<uint32_t>(m >> 29);   // the 23 kept significand bits
+  const uint64_t rest = m & 0x1fffffffull;       // the 29 dropped ones
+  r += static_cast<uint32_t>(rest > 0x10000000ull) | (static_cast<uint32_t>(rest == 0x10000000ull) & (r & 1u));
+  // a carry out of the significand moves the exponent up (to infinity past the range)
+  return float_of(((hi & 0x80000000u) | (static_cast<uint32_t>(e) << 23)) + r);
+}
+
 // a * b rounded to nearest even
 SFP_HD double mul(double a, double b) {
   const uint64_t ab = bits_of(a), bb = bits_of(b);

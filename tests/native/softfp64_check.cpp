@@ -12,6 +12,7 @@ using rkcu::softfp::add;
 using rkcu::softfp::bits_of;
 using rkcu::softfp::double_of;
 using rkcu::softfp::mul;
+using rkcu::softfp::to_float;
 
 static uint64_t s_state;
 static uint64_t next() {  // splitmix64
@@ -39,7 +40,7 @@ static double draw(int kind, double other) {
 int main(int argc, char **argv) {
   const long long count = argc > 1 ? atoll(argv[1]) : 10000000;
   s_state = argc > 2 ? strtoull(argv[2], nullptr, 10) : 1;
-  long long bad_mul = 0, bad_add = 0;
+  long long bad_mul = 0, bad_add = 0, bad_cvt = 0;
   for (long long i = 0; i < count; ++i) {
     const int ka = static_cast<int>(next() % 7);
     const double a = draw(ka == 3 || ka == 4 ? 1 : ka, 0.0);
@@ -55,7 +56,23 @@ int main(int argc, char **argv) {
       if (bad_add++ < 5)
         printf("add %a + %a: hw %a sw %a\n", a, b, pa, sa);
     }
+    // double -> float rounding: the operands, the sum, doubles at the float
+    // range edges, and exact halfway cases
+    const uint64_t r = next();
+    const int ee = (r >> 40) % 2 ? 1023 - 126 - static_cast<int>(r % 3) : 1023 + 127 - static_cast<int>(r % 2);
+    const double cv[4] = {a, pa, double_of((next() & 0x800fffffffffffffull) | (static_cast<uint64_t>(ee) << 52)),
+                          double_of((bits_of(a) & ~0x1fffffffull) | 0x10000000ull)};
+    for (double x : cv) {
+      const float hf = static_cast<float>(x), sf = to_float(x);
+      uint32_t hb, sb;
+      std::memcpy(&hb, &hf, 4);
+      std::memcpy(&sb, &sf, 4);
+      if (!(hf != hf && sf != sf) && hb != sb) {
+        if (bad_cvt++ < 5)
+          printf("to_float %a: hw %a sw %a\n", x, static_cast<double>(hf), static_cast<double>(sf));
+      }
+    }
   }
-  printf("mismatches mul %lld add %lld of %lld\n", bad_mul, bad_add, count);
-  return (bad_mul || bad_add) ? 1 : 0;
+  printf("mismatches mul %lld add %lld to_float %lld of %lld\n", bad_mul, bad_add, bad_cvt, count);
+  return (bad_mul || bad_add || bad_cvt) ? 1 : 0;
 }

@@ -1,6 +1,6 @@
-// Device check of the software binary64 multiply/add (rkcu_softfp64.cuh)
-// against the FP64 pipe's __dmul_rn/__dadd_rn on random and adversarial
-// operands.  Usage: softfp64_check_gpu <count> <seed>; prints mismatches.
+// Device check of the software binary64 multiply/add and double -> float
+// rounding (rkcu_softfp64.cuh) against the FP64 pipe's __dmul_rn/__dadd_rn/
+// __double2float_rn on random and adversarial operands.  Usage: softfp64_check_gpu <count> <seed>; prints mismatches.
 #include <cstdio>
 #include <cstdlib>
 
@@ -28,7 +28,7 @@ __device__ double draw(uint64_t r, int kind, double other) {
 
 __global__ void check(long long count, unsigned long long seed, unsigned long long *bad) {
   const long long stride = (long long)gridDim.x * blockDim.x;
-  unsigned long long bm = 0, ba = 0;
+  unsigned long long bm = 0, ba = 0, bf = 0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += stride) {
     const uint64_t r0 = mix(seed + 4 * i), r1 = mix(seed + 4 * i + 1), r2 = mix(seed + 4 * i + 2),
                    r3 = mix(seed + 4 * i + 3);
@@ -40,20 +40,31 @@ __global__ void check(long long count, unsigned long long seed, unsigned long lo
     const double pa = __dadd_rn(a, b), sa = add(a, b);
     if (!(pm != pm && sm != sm) && bits_of(pm) != bits_of(sm)) ++bm;
     if (!(pa != pa && sa != sa) && bits_of(pa) != bits_of(sa)) ++ba;
+    // conversions: the operands, the sum, and doubles near the float range edges
+    // and halfway cases (the 29 dropped bits exactly 0x10000000)
+    const double near_edge = double_of((r2 & 0x800fffffffffffffull) |
+                                       ((uint64_t)((r0 >> 40) % 2 ? 1023 - 126 - (int)(r1 % 3) : 1023 + 127 - (int)(r1 % 2)) << 52));
+    const double tie = double_of((bits_of(a) & ~0x1fffffffull) | 0x10000000ull);
+    const double cv[4] = {a, pa, near_edge, tie};
+    for (int q = 0; q < 4; ++q) {
+      const float hf = __double2float_rn(cv[q]), sf = to_float(cv[q]);
+      if (!(hf != hf && sf != sf) && __float_as_uint(hf) != __float_as_uint(sf)) ++bf;
+    }
   }
   if (bm) atomicAdd(&bad[0], bm);
   if (ba) atomicAdd(&bad[1], ba);
+  if (bf) atomicAdd(&bad[2], bf);
 }
 
 int main(int argc, char **argv) {
   const long long count = argc > 1 ? atoll(argv[1]) : (1ll << 28);
   const unsigned long long seed = argc > 2 ? strtoull(argv[2], nullptr, 10) : 1;
-  unsigned long long *bad = nullptr, h[2] = {0, 0};
-  if (cudaMalloc(&bad, 2 * sizeof(unsigned long long)) != cudaSuccess) return 2;
-  cudaMemset(bad, 0, 2 * sizeof(unsigned long long));
+  unsigned long long *bad = nullptr, h[3] = {0, 0, 0};
+  if (cudaMalloc(&bad, 3 * sizeof(unsigned long long)) != cudaSuccess) return 2;
+  cudaMemset(bad, 0, 3 * sizeof(unsigned long long));
   check<<<152 * 8, 256>>>(count, seed, bad);
   if (cudaMemcpy(h, bad, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) return 2;
-  printf("mismatches mul %llu add %llu of %lld\n", h[0], h[1], count);
+  printf("mismatches mul %llu add %llu to_float %llu of %lld\n", h[0], h[1], h[2], count);
   cudaFree(bad);
-  return (h[0] || h[1]) ? 1 : 0;
+  return (h[0] || h[1] || h[2]) ? 1 : 0;
 }
