@@ -456,8 +456,10 @@ int rkcu_advance(rkcu_solver *s, int max_steps) {
     m.bruss.N = s->prob.grid_n;
     m.bruss.coef = bruss_coef(&s->prob);
     int grid = 0;
-    // schedule 1 keeps the plain loads (the TMA path needs even N, s <= 8)
-    cudaError_t e = rkcu::launch_mixed(m, s->opt.schedule != 1, s->num_sms, s->stream, &grid);
+    // FP32 stage tiles staged through TMA (even N, s <= 8; else plain loads);
+    // schedule 1 keeps the plain loads
+    const int path = s->opt.schedule == 1 ? rkcu::kMixTiles : rkcu::kMixTilesTma;
+    cudaError_t e = rkcu::launch_mixed(m, path, s->num_sms, s->stream, &grid);
     if (e != cudaSuccess) return cuda_fail(e, "mixed kernel launch");
     s->last_grid = grid;
     ++s->launches;

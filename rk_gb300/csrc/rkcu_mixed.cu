@@ -108,8 +108,8 @@ __device__ __forceinline__ float2 delta_at(const float2 *const *jp, const float 
 }
 
 // kMaxS: an upper bound of the stage count (8 or 13), so that the per-stage
-// loops over earlier stages unroll.
-template <int kMaxS>
+// loops over earlier stages unroll; kPath: how the FP32 stages walk the grid.
+template <int kMaxS, int kPath>
 __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
     mixed_kernel(const __grid_constant__ MixedParams P) {
   // TMA staging buffers: 2 (double buffer) x s slots of kSlotBytes, from the
@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
     s_done = st->done;
     s_step = st->step;
   }
-  if (threadIdx.x == 0 && P.use_tma) {
+  if (threadIdx.x == 0 && kPath == kMixTilesTma) {
     mbar_init(&s_mbar[0], 1);
     mbar_init(&s_mbar[1], 1);
     mbar_fence_init();
@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
         P.y32[p] = make_float2(trunc_to_float(Y.x), trunc_to_float(Y.y));
       }
     }
-    if (P.use_tma) fence_proxy_async_global();  // f0, y32 are read by TMA next
+    if (kPath == kMixTilesTma) fence_proxy_async_global();  // f0, y32 are read by TMA next
     if (!(ok = grid_barrier(st, P.nblocks, P.timeout_ns, 11))) break;
 
     float emax = 0.0f;
@@ -216,15 +216,9 @@ __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
       const float hci = hc[i];
       // dF_i (and, in the last stage, dY, e and y_new) at grid point p from
       // delta_i on the tile (s_delta), y32, and the point's own dF_j / f0
-      auto finish_point = [&](int tr_, int tc_, int k, int j, float2 y32, auto &&own_dF,
-                              auto &&own_f0) {
-        const int p = k * N + j;
+      auto finish_point_at = [&](int p, int k, int j, float2 c, float2 up, float2 dn, float2 w,
+                                 float2 e, float2 y32, auto &&own_dF, auto &&own_f0) {
         const int jcase = j == 0 ? 1 : (j == N - 1 ? 2 : 0);
-        const float2 c = s_delta[tr_ + 1][tc_ + 1];
-        const float2 up = s_delta[k == 0 ? tr_ + 2 : tr_][tc_ + 1];
-        const float2 dn = s_delta[k == N - 1 ? tr_ : tr_ + 2][tc_ + 1];
-        const float2 w = s_delta[tr_ + 1][tc_];
-        const float2 e = s_delta[tr_ + 1][tc_ + 2];
         const float2 dF = delta_rhs(c, up, dn, w, e, jcase, y32, coef);
         if (!last) {
           P.dF[i][p] = dF;
@@ -260,8 +254,15 @@ __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
         emax = fmaxf(emax, dnx == 0.0f ? 3.0e38f : fabsf(er.x) / dnx);
         if (2 * p + 1 < P.n) emax = fmaxf(emax, dny == 0.0f ? 3.0e38f : fabsf(er.y) / dny);
       };
+      auto finish_point = [&](int tr_, int tc_, int k, int j, float2 y32, auto &&own_dF,
+                              auto &&own_f0) {
+        finish_point_at(k * N + j, k, j, s_delta[tr_ + 1][tc_ + 1],
+                        s_delta[k == 0 ? tr_ + 2 : tr_][tc_ + 1],
+                        s_delta[k == N - 1 ? tr_ : tr_ + 2][tc_ + 1], s_delta[tr_ + 1][tc_],
+                        s_delta[tr_ + 1][tc_ + 2], y32, own_dF, own_f0);
+      };
 
-      if (P.use_tma) {
+      if constexpr (kPath == kMixTilesTma) {
         // Tiles through TMA, double-buffered: while tile t is evaluated, the
         // boxes of the CTA's next tile are in flight.  Box slot 0: f0, 1: y32,
         // 1 + j: dF_j for j < i.
@@ -444,17 +445,20 @@ static bool encode_box_map(CUtensorMap *m, const float2 *base, int N) {
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-cudaError_t launch_mixed(const MixedParams &p, bool tma, int num_sms, cudaStream_t stream,
+cudaError_t launch_mixed(const MixedParams &p, int path, int num_sms, cudaStream_t stream,
                          int *grid_out) {
   MixedParams q = p;
-  q.use_tma = 0;
-  if (tma && p.s <= kMixTmaStages) {
+  q.path = path == kMixTilesTma ? kMixTiles : path;
+  if (path == kMixTilesTma && p.s <= kMixTmaStages) {
     bool good = encode_box_map(&q.tm[0], p.f0, p.bruss.N) && encode_box_map(&q.tm[1], p.y32, p.bruss.N);
     for (int j = 1; good && j <= p.s - 2; ++j) good = encode_box_map(&q.tm[1 + j], p.dF[j], p.bruss.N);
-    q.use_tma = good ? 1 : 0;
+    if (good) q.path = kMixTilesTma;
   }
-  const void *kern = p.s <= 8 ? (const void *)mixed_kernel<8> : (const void *)mixed_kernel<kMaxStages>;
-  const size_t dyn = q.use_tma ? 2ull * p.s * kSlotBytes + 128 : 0;
+  // one instantiation per path, so that each gets its own register allocation
+  const void *kern = p.s > 8                  ? (const void *)mixed_kernel<kMaxStages, kMixTiles>
+                     : q.path == kMixTilesTma ? (const void *)mixed_kernel<8, kMixTilesTma>
+                                              : (const void *)mixed_kernel<8, kMixTiles>;
+  const size_t dyn = q.path == kMixTilesTma ? 2ull * p.s * kSlotBytes + 128 : 0;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
   if (e != cudaSuccess) return e;
   int occ = 0;

@@ -24,13 +24,18 @@ struct MixedParams {
   float2 *dF[kMaxStages];  // dF[1 .. s-2]: the stages' right-hand-side increments
   DevState *st;
   Bruss bruss;
-  int use_tma;             // 1: stage tiles through TMA (tm valid), 0: plain loads
+  int path;                // FP32 stages: kMixTilesTma (tm valid) or kMixTiles
   CUtensorMap tm[kMixTmaStages];
 };
 
-// Launches the persistent mixed kernel; tma: stage tiles through TMA where the
-// grid allows it (even N, at most kMixTmaStages stages), else plain loads.
-cudaError_t launch_mixed(const MixedParams &p, bool tma, int num_sms, cudaStream_t stream,
+// How the FP32 stages load their 8 x 32 tiles (with a one-point halo in
+// shared memory): TMA boxes, double-buffered, or plain loads.
+constexpr int kMixTilesTma = 1, kMixTiles = 2;
+
+// Launches the persistent mixed kernel with the given kMix* path (kMixTilesTma
+// falls back to kMixTiles where TMA boxes do not fit: odd N or more than
+// kMixTmaStages stages).
+cudaError_t launch_mixed(const MixedParams &p, int path, int num_sms, cudaStream_t stream,
                          int *grid_out);
 
 }  // namespace rkcu

@@ -37,8 +37,11 @@ def test_lowstorage_n2000_matches_reference_with_less_memory():
     assert (st["steps_acc"], st["steps_rej"]) == (rec["accepted"], rec["rejected"])
     assert hashlib.sha256(y.astype("<f8").tobytes()).hexdigest() == rec["y_sha256"]
     n = rec["n"]
-    # 2n state doubles + the ring window, far below the plain form's (s+3) n
-    assert ls_bytes < 0.4 * (7 + 3) * n * 8
+    # 2n state doubles + the ring window: 2n + (s^2 + 5s - 4) R 2N doubles with
+    # blocks of R = 64 rows (128 MB + 164 MB), against the plain form's (s+3) n
+    N, s, R = rec["grid_n"], 7, 64
+    assert ls_bytes == (2 * n + (s * s + 5 * s - 4) * R * 2 * N) * 8
+    assert ls_bytes < 0.5 * (s + 3) * n * 8
     print(f"low-storage device bytes {ls_bytes / 1e6:.0f} MB vs plain {(7 + 3) * n * 8 / 1e6:.0f} MB")
 
 

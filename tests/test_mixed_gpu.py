@@ -55,25 +55,27 @@ def test_mixed_rejects_problems_without_a_mixed_evaluator():
 
 
 @pytest.mark.parametrize("N,method", [(64, "DOPRI54"), (250, "DOPRI54"), (48, "RKF23"),
-                                      (40, "DOPRI87")])
+                                      (40, "DOPRI87"), (37, "DOPRI54")])
 def test_mixed_tma_staging_equals_plain_loads(N, method):
-    """The FP32 stages read their tiles either through TMA boxes staged in shared
-    memory (even N, at most 8 stages) or with plain loads (schedule 1); both
-    evaluate the same operations on the same values, so the bits agree."""
+    """The FP32 stages read their tiles through TMA boxes staged in shared
+    memory (default; even N, at most 8 stages, else plain loads) or with plain
+    loads (schedule 1); both evaluate the same operations on the same values,
+    so the bits agree."""
     prob = rk.bruss2d_mix(N, 2e-3)
     y0 = rk.ode_start(prob)
     out = []
     for sched in (0, 1):
         with rk.Solver(prob, method=method, precision="mixed", schedule=sched) as s:
             out.append(s.solve(0.0, 0.1, y0, 1e-6))
-    (a, sa), (b, sb) = out
-    assert (sa["steps_acc"], sa["steps_rej"]) == (sb["steps_acc"], sb["steps_rej"])
-    np.testing.assert_array_equal(a, b)
+    (a, sa) = out[0]
+    for b, sb in out[1:]:
+        assert (sa["steps_acc"], sa["steps_rej"]) == (sb["steps_acc"], sb["steps_rej"])
+        np.testing.assert_array_equal(a, b)
 
 
-def test_mixed_odd_grid_uses_plain_loads():
-    """An odd N cannot use TMA boxes (rows would not be 16-byte aligned); the
-    kernel falls back to plain loads and stays within the tolerance of FP64."""
+def test_mixed_odd_grid_within_tolerance():
+    """An odd N (no TMA boxes: rows would not be 16-byte aligned) stays within
+    the tolerance of the FP64 path."""
     N = 37
     prob = rk.bruss2d_mix(N, 2e-3)
     y0 = rk.ode_start(prob)
