@@ -31,11 +31,14 @@ extern "C" {
 #define RKCU_ERR_STATE        -5   /* call out of order (e.g. advance before begin) */
 #define RKCU_ERR_NO_DEVICE    -6   /* no CUDA device, or not an sm_103 device */
 #define RKCU_ERR_TOO_LARGE    -7   /* system larger than rkcu_solve_noalloc accepts */
+#define RKCU_ERR_RHS          -8   /* the caller's right-hand side (rkcu_set_rhs) failed */
 
 /* ---- problems (include/ode.h modules) ---------------------------------- */
 #define RKCU_PROBLEM_BRUSS2D_MIX  0   /* src/problems/bruss2d-mix.c */
 #define RKCU_PROBLEM_LV_PAIRS     1   /* src/problems/lv.c */
 #define RKCU_PROBLEM_LV_BANDED    2   /* banded Lotka-Volterra chain (no reference module) */
+#define RKCU_PROBLEM_RHS          3   /* any ode_eval_rng: a device function the caller supplies
+                                         through rkcu_set_rhs (only n is used) */
 
 /* ---- arithmetic -------------------------------------------------------- */
 #define RKCU_FP64_EXACT  0   /* reference evaluation order, no contraction, and the C
@@ -115,6 +118,27 @@ int rkcu_set_method(rkcu_solver *s, double **A, const double *b, const double *b
 /* Same, for the tableaux of src/methods.c by name: "HEUN2", "RK4", "SSPRK3",
    "RKF23", "DOPRI54", "VERNER65", "DOPRI87". */
 int rkcu_set_method_by_name(rkcu_solver *s, const char *name);
+
+/* General right-hand side, for problems whose ode_eval_rng reaches beyond a
+   limited access distance (the reference's A/E/F variants, src/impl/seq/A.c,
+   serve those; the fused kernels here need the BRUSS2D-MIX/LV stencils).  The
+   function evaluates f(t, w) for all n components on the device: w and f are
+   device arrays of n doubles (16-byte aligned, with one spare element when n
+   is odd), and the work must be enqueued on `stream` (the solver's
+   cudaStream_t).  It returns 0, or nonzero to stop the solve with RKCU_ERR_RHS.
+   A solver for RKCU_PROBLEM_RHS runs the step loop of src/impl/seq/A.c:57-85
+   around it: per stage a combine kernel w_l = y + sum_j h a_lj F_j, the call
+   f(t + h c_l, w_l), then an output kernel for dy, err, y and the error max and
+   a one-thread step-control kernel; the host reads the state back once per
+   step.  FP64 modes only (RKCU_FP64_EXACT: the reference's rounding), plain
+   variant. */
+typedef int (*rkcu_rhs_fn)(double t, const double *w, double *f, int n, void *stream, void *user);
+int rkcu_set_rhs(rkcu_solver *s, rkcu_rhs_fn fn, void *user);
+/* A right-hand side of that form for the built-in modules, with `user` a
+   const rkcu_problem * of RKCU_PROBLEM_BRUSS2D_MIX or RKCU_PROBLEM_LV_PAIRS
+   (ode_eval_rng of src/problems/bruss2d-mix.c:670-712, src/problems/lv.c:89-121,
+   in the reference's rounding). */
+int rkcu_rhs_builtin(double t, const double *w, double *f, int n, void *stream, void *user);
 /* Read a built-in tableau: A row-major [stages*stages]; arrays need 16 entries.
    Returns RKCU_ERR_INVALID for an unknown name.  HAS_EMB_SOL (methods.h:95-118)
    is returned in *embedded. */

@@ -28,10 +28,12 @@ ERR_TIMEOUT = -4
 ERR_STATE = -5
 ERR_NO_DEVICE = -6
 ERR_TOO_LARGE = -7
+ERR_RHS = -8
 
 PROBLEM_BRUSS2D_MIX = 0
 PROBLEM_LV_PAIRS = 1
 PROBLEM_LV_BANDED = 2
+PROBLEM_RHS = 3
 
 FP64_EXACT = 0
 FP64_FMA = 1
@@ -56,8 +58,12 @@ EXPORTS = (
     "rkcu_batch_footprint", "rkcu_batch_create", "rkcu_batch_destroy", "rkcu_batch_add",
     "rkcu_batch_run", "rkcu_batch_finished", "rkcu_batch_take", "rkcu_batch_tune",
     "rkcu_batch_set_tuning", "rkcu_batch_get_tuning", "rkcu_batch_info", "rkcu_batch_stream",
-    "rkcu_set_trace", "rkcu_get_trace",
+    "rkcu_set_trace", "rkcu_get_trace", "rkcu_set_rhs", "rkcu_rhs_builtin",
 )
+
+# int rhs(double t, const double *w, double *f, int n, void *stream, void *user)
+RHS_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_double, ctypes.c_void_p, ctypes.c_void_p,
+                          ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p)
 
 
 class RkcuError(RuntimeError):
@@ -134,6 +140,7 @@ def load():
     lib.rkcu_step_size.argtypes = [D, D, D, I, P(I)]
     lib.rkcu_step_sizes_device.argtypes = [V, V, I, D, I, V, V]
     lib.rkcu_run.argtypes = [V, I, P(Stats)]
+    lib.rkcu_set_rhs.argtypes = [V, V, V]
     lib.rkcu_set_trace.argtypes = [V, I, I]
     lib.rkcu_get_trace.argtypes = [V, V, V, V, V, I, P(I)]
     LL = ctypes.c_longlong
@@ -184,7 +191,22 @@ class ProblemSpec:
     @property
     def name(self):
         return {PROBLEM_BRUSS2D_MIX: "bruss2d-mix", PROBLEM_LV_PAIRS: "lv-pairs",
-                PROBLEM_LV_BANDED: "lv-banded"}[self.kind]
+                PROBLEM_LV_BANDED: "lv-banded", PROBLEM_RHS: "rhs"}[self.kind]
+
+
+def rhs_problem(n):
+    """A system of n components whose right-hand side the caller supplies
+    (Solver.set_rhs): any ode_eval_rng, without a limited access distance."""
+    return ProblemSpec(PROBLEM_RHS, n)
+
+
+class DeviceArray:
+    """A device array of n doubles at a raw address, for torch.as_tensor (the
+    CUDA array interface); lets a Python right-hand side work on w and f."""
+
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<f8", "data": (ptr, False),
+                                         "version": 3, "strides": None}
 
 
 def bruss2d_mix(grid_n, alpha=2e-3):
@@ -362,6 +384,31 @@ class Solver:
         y = np.empty(self.problem.n)
         _check(self._lib.rkcu_get_y(self._h, _ptr(y), 0), "rkcu_get_y")
         return y
+
+    def set_rhs(self, fn, user=None):
+        """The right-hand side of a rhs_problem: "builtin" with user a BRUSS2D-MIX
+        or LV-pairs ProblemSpec (rkcu_rhs_builtin), or a Python callable
+        fn(t, w_ptr, f_ptr, n, stream) that enqueues f = f(t, w) on the given
+        stream and returns 0 (nonzero stops the solve with ERR_RHS)."""
+        if isinstance(fn, str) and fn == "builtin":
+            ps = user.cstruct()
+            self._rhs_keep = (ps, user)
+            fptr = ctypes.cast(self._lib.rkcu_rhs_builtin, ctypes.c_void_p)
+            uptr = ctypes.cast(ctypes.pointer(ps), ctypes.c_void_p)
+            _check(self._lib.rkcu_set_rhs(self._h, fptr, uptr), "rkcu_set_rhs")
+            return
+
+        def tramp(t, w, f, n, stream, _user):
+            try:
+                return int(fn(t, w, f, n, stream) or 0)
+            except Exception:  # a Python exception must not cross the C boundary
+                import traceback
+                traceback.print_exc()
+                return 1
+
+        cb = RHS_FN(tramp)
+        self._rhs_keep = (cb,)
+        _check(self._lib.rkcu_set_rhs(self._h, ctypes.cast(cb, ctypes.c_void_p), None), "rkcu_set_rhs")
 
     def set_trace(self, capacity, with_y=False):
         """Record the first `capacity` attempted steps after each begin: t, h,

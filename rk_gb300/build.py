@@ -23,7 +23,7 @@ OBJDIR = os.path.join(PKG, "_build")
 INCLUDE = os.path.join(REPO, "include")
 
 CU_SOURCES = ["rkcu_api.cu", "rkcu_plain.cu", "rkcu_methods.cu", "rkcu_noalloc.cu", "rkcu_mixed.cu",
-              "rkcu_batch.cu", "rkcu_batch_api.cu", "rkcu_lowstorage.cu"]
+              "rkcu_batch.cu", "rkcu_batch_api.cu", "rkcu_lowstorage.cu", "rkcu_general.cu"]
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 
 

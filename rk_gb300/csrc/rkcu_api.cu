@@ -9,6 +9,7 @@
 #include <new>
 
 #include "rkcu.h"
+#include "rkcu_general.cuh"
 #include "rkcu_lowstorage.cuh"
 #include "rkcu_mixed.cuh"
 #include "rkcu_plain.cuh"
@@ -68,7 +69,10 @@ struct rkcu_solver {
   bool have_method = false;
   int s = 0, ord = 0;
   double A[kMaxStages * kMaxStages] = {};
-  double b[kMaxStages] = {}, bh[kMaxStages] = {};
+  double b[kMaxStages] = {}, bh[kMaxStages] = {}, c[kMaxStages] = {};
+  // caller's right-hand side (RKCU_PROBLEM_RHS)
+  rkcu_rhs_fn rhs = nullptr;
+  void *rhs_user = nullptr;
   // device memory
   size_t npairs = 0;
   double2 *y[2] = {nullptr, nullptr};
@@ -116,6 +120,58 @@ static void flow_geometry(const rkcu_solver *s, int *tile, int *ntiles, int *dep
   *dep = d;
 }
 
+// The step loop of src/impl/seq/A.c:57-85 around the caller's right-hand side:
+// stage vectors F_0..F_{s-1} and w in the solver's stage storage, one state
+// read-back per step (the host passes t + h c_l to the function).  Stops after
+// a step whose size update is left to the host, as the fused kernels do.
+static int advance_rhs(rkcu_solver *s, int max_steps) {
+  const int mode = s->opt.precision == RKCU_FP64_EXACT        ? rkcu::kArithExactSoftMul
+                   : s->opt.precision == RKCU_FP64_EXACT_HWMUL ? rkcu::kArithExact
+                                                               : rkcu::kArithFused;
+  const size_t ld = 2 * s->npairs;  // doubles per stage vector
+  double *F = reinterpret_cast<double *>(s->stage);
+  double *w = F + (size_t)s->s * ld;
+  const long long n = s->prob.n;
+  DevState *h = s->st_host;
+  rkcu::GenCoef cf;
+  std::memset(&cf, 0, sizeof(cf));
+  cf.s = s->s;
+  for (int k = 0; k < max_steps; ++k) {
+    if (h->done || h->pending || h->error) break;
+    // premult (src/methods.c:43-58)
+    const double hh = h->h, t = h->t;
+    double hc[kMaxStages];
+    for (int i = 0; i < s->s; ++i) {
+      for (int j = 0; j < i; ++j) {
+        cf.hA[i * kMaxStages + j] = hh * s->A[i * kMaxStages + j];
+        cf.nzA[i * kMaxStages + j] = s->A[i * kMaxStages + j] != 0.0;
+      }
+      cf.hb[i] = hh * s->b[i];
+      cf.hbh[i] = hh * s->bh[i];
+      cf.nzb[i] = s->b[i] != 0.0;
+      cf.nzbh[i] = s->bh[i] != 0.0;
+      hc[i] = hh * s->c[i];
+    }
+    const double *ycur = reinterpret_cast<const double *>(s->y[h->cur & 1]);
+    double *ynew = reinterpret_cast<double *>(s->y[(h->cur & 1) ^ 1]);
+    if (s->rhs(t + hc[0], ycur, F, (int)n, (void *)s->stream, s->rhs_user) != 0) return RKCU_ERR_RHS;
+    for (int l = 1; l < s->s; ++l) {
+      cudaError_t e = rkcu::launch_gen_combine(cf, l, ycur, F, ld, w, n, mode, s->num_sms, s->stream);
+      if (e != cudaSuccess) return cuda_fail(e, "combine kernel");
+      if (s->rhs(t + hc[l], w, F + (size_t)l * ld, (int)n, (void *)s->stream, s->rhs_user) != 0)
+        return RKCU_ERR_RHS;
+    }
+    cudaError_t e = rkcu::launch_gen_output(cf, ycur, F, ld, ynew, n, s->st, mode, s->num_sms, s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "output kernel");
+    e = rkcu::launch_gen_control(s->st, s->tol, s->ord, s->te, s->opt.step_limit, s->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "step control kernel");
+    s->launches += s->s + 1;
+    RKCU_CK(cudaMemcpyAsync(h, s->st, sizeof(DevState), cudaMemcpyDeviceToHost, s->stream));
+    RKCU_CK(cudaStreamSynchronize(s->stream));
+  }
+  return RKCU_OK;
+}
+
 extern "C" {
 
 void rkcu_options_default(rkcu_options *o) {
@@ -140,6 +196,7 @@ const char *rkcu_strerror(int status) {
     case RKCU_ERR_STATE: return "call out of order";
     case RKCU_ERR_NO_DEVICE: return "no usable CUDA device";
     case RKCU_ERR_TOO_LARGE: return "system larger than the allocation-free limit (65536 components)";
+    case RKCU_ERR_RHS: return "the caller's right-hand side failed";
     default: return "unknown status";
   }
 }
@@ -170,7 +227,8 @@ int rkcu_destroy(rkcu_solver *s) {
 int rkcu_create(rkcu_solver **out, const rkcu_problem *prob, const rkcu_options *opt) {
   if (!out) return RKCU_ERR_INVALID;
   *out = nullptr;
-  int rc = check_problem(prob);
+  const bool general = prob && prob->problem == RKCU_PROBLEM_RHS;
+  int rc = general ? (prob->n > 0 ? RKCU_OK : RKCU_ERR_INVALID) : check_problem(prob);
   if (rc != RKCU_OK) return rc;
   rkcu_options o;
   if (opt)
@@ -181,6 +239,7 @@ int rkcu_create(rkcu_solver **out, const rkcu_problem *prob, const rkcu_options 
       o.precision != RKCU_FP64_EXACT_HWMUL)
     return RKCU_ERR_INVALID;
   if (o.precision == RKCU_MIXED && prob->problem != RKCU_PROBLEM_BRUSS2D_MIX) return RKCU_ERR_INVALID;
+  if (general && o.variant != RKCU_VARIANT_D) return RKCU_ERR_INVALID;
   if (o.variant != RKCU_VARIANT_D && o.variant != RKCU_VARIANT_LOWSTORAGE) return RKCU_ERR_INVALID;
   if (o.variant == RKCU_VARIANT_LOWSTORAGE &&
       (prob->problem != RKCU_PROBLEM_BRUSS2D_MIX || o.precision == RKCU_MIXED || o.block_rows < 0))
@@ -255,17 +314,20 @@ int rkcu_create(rkcu_solver **out, const rkcu_problem *prob, const rkcu_options 
 
 int rkcu_set_method(rkcu_solver *s, double **A, const double *b, const double *b_hat,
                     const double *c, int stages, int ord) {
-  (void)c;  // BRUSS2D-MIX and LV are autonomous: c only enters through t + h*c_i
+  // c enters only through t + h c_l, which the autonomous built-in modules
+  // ignore; a caller's right-hand side receives it (RKCU_PROBLEM_RHS)
   if (!s || !A || !b || !b_hat || stages < 2 || stages > kMaxStages || ord < 1)
     return RKCU_ERR_INVALID;
   std::memset(s->A, 0, sizeof(s->A));
   std::memset(s->b, 0, sizeof(s->b));
   std::memset(s->bh, 0, sizeof(s->bh));
+  std::memset(s->c, 0, sizeof(s->c));
   for (int i = 0; i < stages; ++i) {
     if (!A[i]) return RKCU_ERR_INVALID;
     for (int j = 0; j < i; ++j) s->A[i * kMaxStages + j] = A[i][j];
     s->b[i] = b[i];
     s->bh[i] = b[i] - b_hat[i];  // src/impl/seq/D.c:40-41
+    s->c[i] = c ? c[i] : 0.0;
   }
   s->s = stages;
   s->ord = ord;
@@ -290,6 +352,7 @@ int rkcu_begin(rkcu_solver *s, double t0, double te, const double *y0, int y0_on
   if (!s || !y0 || !s->have_method) return s ? RKCU_ERR_STATE : RKCU_ERR_INVALID;
   if (!(te == te) || !(t0 == t0)) return RKCU_ERR_INVALID;
   if (tol <= 0.0 && s->opt.step_limit <= 0) return RKCU_ERR_INVALID;  // fixed step needs a limit
+  if (s->prob.problem == RKCU_PROBLEM_RHS && !s->rhs) return RKCU_ERR_STATE;
   RKCU_CK(cudaSetDevice(s->opt.device));
   if (s->opt.precision == RKCU_MIXED) {
     const int mneed = s->s;  // f0, y32, dF[1..s-2]
@@ -372,6 +435,7 @@ int rkcu_advance(rkcu_solver *s, int max_steps) {
   if (!s->begun) return RKCU_ERR_STATE;
   if (max_steps <= 0) return RKCU_OK;
   RKCU_CK(cudaSetDevice(s->opt.device));
+  if (s->prob.problem == RKCU_PROBLEM_RHS) return advance_rhs(s, max_steps);
   if (s->opt.variant == RKCU_VARIANT_LOWSTORAGE) {
     rkcu::LsParams q;
     std::memset(&q, 0, sizeof(q));
@@ -642,10 +706,32 @@ int rkcu_debug_inject_wait_timeout(rkcu_solver *s, int extra_arrivals) {
   return RKCU_OK;
 }
 
+int rkcu_set_rhs(rkcu_solver *s, rkcu_rhs_fn fn, void *user) {
+  if (!s || !fn || s->prob.problem != RKCU_PROBLEM_RHS) return RKCU_ERR_INVALID;
+  s->rhs = fn;
+  s->rhs_user = user;
+  s->begun = false;
+  return RKCU_OK;
+}
+
+int rkcu_rhs_builtin(double t, const double *w, double *f, int n, void *stream, void *user) {
+  (void)t;  // both modules are autonomous
+  const rkcu_problem *prob = static_cast<const rkcu_problem *>(user);
+  if (!prob || !w || !f || prob->n != n || check_problem(prob) != RKCU_OK ||
+      prob->problem == RKCU_PROBLEM_LV_BANDED)
+    return RKCU_ERR_INVALID;
+  const rkcu::Bruss br{prob->grid_n, prob->problem == RKCU_PROBLEM_BRUSS2D_MIX ? bruss_coef(prob) : 0.0};
+  const rkcu::LvBanded lvb{};
+  const cudaError_t e = rkcu::launch_eval_rhs(prob->problem, br, lvb, (n + 1) / 2,
+                                              reinterpret_cast<const double2 *>(w),
+                                              reinterpret_cast<double2 *>(f), static_cast<cudaStream_t>(stream));
+  return e == cudaSuccess ? RKCU_OK : cuda_fail(e, "built-in right-hand side");
+}
+
 int rkcu_set_trace(rkcu_solver *s, int capacity, int with_y) {
   if (!s || capacity < 0) return RKCU_ERR_INVALID;
-  if (capacity > 0 &&
-      (s->opt.variant != RKCU_VARIANT_D || s->opt.precision == RKCU_MIXED))
+  if (capacity > 0 && (s->opt.variant != RKCU_VARIANT_D || s->opt.precision == RKCU_MIXED ||
+                       s->prob.problem == RKCU_PROBLEM_RHS))
     return RKCU_ERR_INVALID;
   RKCU_CK(cudaSetDevice(s->opt.device));
   RKCU_CK(cudaStreamSynchronize(s->stream));
