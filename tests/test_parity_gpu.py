@@ -171,6 +171,31 @@ def test_wait_timeout_is_reported_and_recoverable():
     assert st["steps_acc"] + st["steps_rej"] == rec["steps"]
 
 
+@pytest.mark.parametrize("cfg", [dict(schedule=2), dict(schedule=3),
+                                 dict(variant=rk.VARIANT_LOWSTORAGE), dict(precision="mixed"),
+                                 dict(precision="mixed", schedule=1)],
+                         ids=["neighbour-flags", "flow-tiles", "low-storage", "mixed-tma",
+                              "mixed-plain-loads"])
+def test_wait_timeout_in_every_persistent_kernel(cfg):
+    """Each persistent kernel's bounded waits end with RKCU_ERR_TIMEOUT when CTAs
+    that never exist are awaited; the next solve on the same solver then equals
+    a fresh solver's result bit for bit."""
+    prob = rk.bruss2d_mix(16, 1e-2)
+    y0 = rk.ode_start(prob)
+    kw = dict(method="DOPRI54", **cfg)
+    with rk.Solver(prob, **kw) as ref_solver:
+        ref, rst = ref_solver.solve(0.0, 0.3, y0, 1e-7)
+    with rk.Solver(prob, wait_timeout_s=0.2, **kw) as s:
+        s.inject_wait_timeout(1)
+        with pytest.raises(rk.RkcuError) as ei:
+            s.solve(0.0, 0.3, y0, 1e-7)
+        assert ei.value.status == rk.ERR_TIMEOUT
+        s.inject_wait_timeout(0)
+        y, st = s.solve(0.0, 0.3, y0, 1e-7)
+    assert (st["steps_acc"], st["steps_rej"]) == (rst["steps_acc"], rst["steps_rej"])
+    np.testing.assert_array_equal(y, ref)
+
+
 def test_bad_calls_are_rejected():
     prob = rk.bruss2d_mix(8)
     with rk.Solver(prob, method="RK4") as s:
