@@ -75,7 +75,7 @@ def fp64_ops_per_comp(method, precision):
     right-hand side with its max/compare work).  The mixed form keeps only F0
     (7.5), the FP64 update (2) and two conversions."""
     if precision == "mixed":
-        return 12.0, 12.0
+        return 10.0, 12.0
     import rk_gb300 as rk
     m = rk.builtin_method(method)
     s = m["s"]

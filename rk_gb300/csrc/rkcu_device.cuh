@@ -30,6 +30,10 @@ constexpr int kMaxStages = 13;   // DOPRI87 (src/methods.c:476) is the largest t
 constexpr int kArithFused = 0;
 constexpr int kArithExact = 1;
 constexpr int kArithExactSoftMul = 2;
+// kArithFusedSoftMul (3): as kArithFused (a*b+c contracted into FMAs), with the
+// products that stay plain products computed in software binary64 on the
+// integer pipe -- the same bits as kArithFused, fewer FP64 instructions.
+constexpr int kArithFusedSoftMul = 3;
 
 template <int kMode>
 struct Arith;
@@ -47,6 +51,10 @@ struct Arith<kArithExact> {
   static __device__ __forceinline__ double msub(double a, double b, double c) {
     return __dsub_rn(__dmul_rn(a, b), c);
   }
+  // x - a*b with the product rounded first
+  static __device__ __forceinline__ double submul(double x, double a, double b) {
+    return __dsub_rn(x, __dmul_rn(a, b));
+  }
 };
 
 template <>
@@ -60,6 +68,19 @@ struct Arith<kArithExactSoftMul> {
   static __device__ __forceinline__ double msub(double a, double b, double c) {
     return __dsub_rn(softfp::mul(a, b), c);
   }
+  static __device__ __forceinline__ double submul(double x, double a, double b) {
+    return __dsub_rn(x, softfp::mul(a, b));
+  }
+};
+
+template <>
+struct Arith<kArithFusedSoftMul> {
+  static __device__ __forceinline__ double mul(double a, double b) { return softfp::mul(a, b); }
+  static __device__ __forceinline__ double add(double a, double b) { return a + b; }
+  static __device__ __forceinline__ double sub(double a, double b) { return a - b; }
+  static __device__ __forceinline__ double mac(double acc, double a, double b) { return fma(a, b, acc); }
+  static __device__ __forceinline__ double msub(double a, double b, double c) { return fma(a, b, -c); }
+  static __device__ __forceinline__ double submul(double x, double a, double b) { return fma(-a, b, x); }
 };
 
 template <>
@@ -69,6 +90,7 @@ struct Arith<kArithFused> {
   static __device__ __forceinline__ double sub(double a, double b) { return a - b; }
   static __device__ __forceinline__ double mac(double acc, double a, double b) { return fma(a, b, acc); }
   static __device__ __forceinline__ double msub(double a, double b, double c) { return fma(a, b, -c); }
+  static __device__ __forceinline__ double submul(double x, double a, double b) { return fma(-a, b, x); }
 };
 
 // ---------------------------------------------------------------------------
@@ -131,7 +153,7 @@ struct Bruss {
     lu = fma(-4.0, c.x, lu);
     lv = fma(-4.0, c.y, lv);
     const double u2v = M::mul(M::mul(c.x, c.x), c.y);  // shared by U and V
-    const double ru = M::sub(M::add(1.0, u2v), M::mul(4.4, c.x));
+    const double ru = M::submul(M::add(1.0, u2v), 4.4, c.x);
     const double rv = M::msub(3.4, c.x, u2v);
     return make_double2(M::mac(ru, coef, lu), M::mac(rv, coef, lv));
   }

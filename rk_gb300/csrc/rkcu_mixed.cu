@@ -191,7 +191,7 @@ __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
     {
       const double hbs = s_hbsum;
       for (int p = gtid; p < P.npairs; p += gstride) {
-        const double2 F = br.eval<kArithFused>(ycur, p);
+        const double2 F = br.eval<kArithFusedSoftMul>(ycur, p);
         const double2 Y = ycur[p];
         ynew[p] = make_double2(fma(hbs, F.x, Y.x), fma(hbs, F.y, Y.y));
         // rounded to float on the integer pipe (the conversion instruction would
