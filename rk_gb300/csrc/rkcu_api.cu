@@ -575,9 +575,10 @@ int rkcu_advance(rkcu_solver *s, int max_steps) {
   p.lvb.a = s->lv_a;
   p.extra_arrivals = s->extra_arrivals;
   int grid = 0;
+  // FMA mode: the fused arithmetic with its plain products in software (same bits)
   const int mode = s->opt.precision == RKCU_FP64_EXACT        ? rkcu::kArithExactSoftMul
                    : s->opt.precision == RKCU_FP64_EXACT_HWMUL ? rkcu::kArithExact
-                                                               : rkcu::kArithFused;
+                                                               : rkcu::kArithFusedSoftMul;
   cudaError_t e = rkcu::launch_plain(p, mode, 0, s->num_sms, s->stream, &grid);
   if (e != cudaSuccess) return cuda_fail(e, "plain kernel launch");
   s->last_grid = grid;

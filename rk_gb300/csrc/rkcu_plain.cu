@@ -352,6 +352,8 @@ static cudaError_t launch_mode(const PlainParams &p, int mode, int blocks_per_sm
     case kArithExact: return launch_one<Prob, kArithExact>(p, blocks_per_sm, num_sms, stream, grid_out);
     case kArithExactSoftMul:
       return launch_one<Prob, kArithExactSoftMul>(p, blocks_per_sm, num_sms, stream, grid_out);
+    case kArithFusedSoftMul:
+      return launch_one<Prob, kArithFusedSoftMul>(p, blocks_per_sm, num_sms, stream, grid_out);
     default: return launch_one<Prob, kArithFused>(p, blocks_per_sm, num_sms, stream, grid_out);
   }
 }
