@@ -240,12 +240,12 @@ static int grid_of(int blocks_per_sm, int num_sms) {
 int batch_grid(bool exact, int threads, int blocks_per_sm, int num_sms) {
   if (threads == 128)
     return exact ? grid_of<kArithExactSoftMul, 128>(blocks_per_sm, num_sms)
-                 : grid_of<kArithFused, 128>(blocks_per_sm, num_sms);
+                 : grid_of<kArithFusedSoftMul, 128>(blocks_per_sm, num_sms);
   if (threads == 512)
     return exact ? grid_of<kArithExactSoftMul, 512>(blocks_per_sm, num_sms)
-                 : grid_of<kArithFused, 512>(blocks_per_sm, num_sms);
+                 : grid_of<kArithFusedSoftMul, 512>(blocks_per_sm, num_sms);
   return exact ? grid_of<kArithExactSoftMul, 256>(blocks_per_sm, num_sms)
-               : grid_of<kArithFused, 256>(blocks_per_sm, num_sms);
+               : grid_of<kArithFusedSoftMul, 256>(blocks_per_sm, num_sms);
 }
 
 template <int kExact, int kT>
@@ -271,10 +271,10 @@ cudaError_t launch_batch(const BatchParams &p, bool exact, int threads, int bloc
   if (grid <= 0) return cudaErrorInvalidConfiguration;
   *grid_out = grid;
   if (threads == 128)
-    return exact ? launch_t<kArithExactSoftMul, 128>(p, grid, stream) : launch_t<kArithFused, 128>(p, grid, stream);
+    return exact ? launch_t<kArithExactSoftMul, 128>(p, grid, stream) : launch_t<kArithFusedSoftMul, 128>(p, grid, stream);
   if (threads == 512)
-    return exact ? launch_t<kArithExactSoftMul, 512>(p, grid, stream) : launch_t<kArithFused, 512>(p, grid, stream);
-  return exact ? launch_t<kArithExactSoftMul, 256>(p, grid, stream) : launch_t<kArithFused, 256>(p, grid, stream);
+    return exact ? launch_t<kArithExactSoftMul, 512>(p, grid, stream) : launch_t<kArithFusedSoftMul, 512>(p, grid, stream);
+  return exact ? launch_t<kArithExactSoftMul, 256>(p, grid, stream) : launch_t<kArithFusedSoftMul, 256>(p, grid, stream);
 }
 
 }  // namespace rkcu

@@ -256,7 +256,7 @@ static cudaError_t launch_t(const LsParams &p, int num_sms, cudaStream_t stream,
 cudaError_t launch_lowstorage(const LsParams &p, bool exact, int num_sms, cudaStream_t stream,
                               int *grid_out) {
   return exact ? launch_t<kArithExactSoftMul>(p, num_sms, stream, grid_out)
-               : launch_t<kArithFused>(p, num_sms, stream, grid_out);
+               : launch_t<kArithFusedSoftMul>(p, num_sms, stream, grid_out);
 }
 
 size_t lowstorage_ring_pairs(int s, int R, int N) {

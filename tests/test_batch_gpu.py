@@ -35,9 +35,9 @@ def _mix(seed=3):
     return items
 
 
-def _run_batch(items, tune=False, graph=True, sweeps=64):
+def _run_batch(items, tune=False, graph=True, sweeps=64, precision="exact"):
     out = {}
-    with rk.Batch(1 * GB, 64) as b:
+    with rk.Batch(1 * GB, 64, precision=precision) as b:
         if not graph:
             b.set_tuning(256, 512, 0, use_graph=False)
         for k, (p, y0, t0, te, tol) in enumerate(items):
@@ -80,6 +80,20 @@ def test_batch_agrees_with_oracle(oracle):
     # the batch keeps the correctly rounded step-size factor; it differs from the C
     # library's only in rare near-halfway cases, so nearly every instance is identical
     assert identical >= 0.8 * len(items), identical
+
+
+def test_fma_mode_within_tolerance_and_independent_of_the_mix(oracle):
+    """FMA mode (products that stay products in software, the rest fused):
+    each instance within its tolerance of the oracle, and alone = in the mix."""
+    items = _mix(seed=5)[:10] + _mix(seed=5)[18:20]
+    res = _run_batch(items, precision="fma")
+    for k, (p, y0, t0, te, tol) in enumerate(items):
+        kind = {rk.PROBLEM_BRUSS2D_MIX: oracle.BRUSS2D_MIX, rk.PROBLEM_LV_PAIRS: oracle.LV_PAIRS}[p.kind]
+        ref, _ = oracle.solve(kind, y0, "DOPRI54", t0, te, tol, grid_n=p.grid_n, alpha=p.alpha)
+        y, _ = res[k]
+        assert float(np.max(np.abs(y - ref)) / np.max(np.abs(ref))) <= 10 * tol
+    alone = _run_batch(items[:1], precision="fma")[0]
+    np.testing.assert_array_equal(res[0][0], alone[0])
 
 
 def test_tuning_and_graph_replay_change_nothing():

@@ -45,6 +45,20 @@ def test_lowstorage_n2000_matches_reference_with_less_memory():
     print(f"low-storage device bytes {ls_bytes / 1e6:.0f} MB vs plain {(7 + 3) * n * 8 / 1e6:.0f} MB")
 
 
+@pytest.mark.parametrize("method", ["DOPRI54", "DOPRI87"])
+def test_lowstorage_fma_equals_plain_fma(method):
+    """The FMA mode applies the same operations per component in both forms."""
+    prob = rk.bruss2d_mix(64, 5e-3)
+    y0 = rk.ode_start(prob)
+    out = []
+    for variant in (rk.VARIANT_D, rk.VARIANT_LOWSTORAGE):
+        with rk.Solver(prob, method=method, precision="fma", variant=variant) as s:
+            out.append(s.solve(0.0, 0.2, y0, 1e-7))
+    (a, sa), (b, sb) = out
+    assert (sa["steps_acc"], sa["steps_rej"]) == (sb["steps_acc"], sb["steps_rej"])
+    np.testing.assert_array_equal(a, b)
+
+
 def test_lowstorage_rejects_other_problems():
     with pytest.raises(rk.RkcuError) as ei:
         rk.Solver(rk.lv_pairs(10), variant=rk.VARIANT_LOWSTORAGE)
