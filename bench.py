@@ -348,6 +348,7 @@ def run_ours(args):
                           "unit": "G FP64 instr/s", "frac": fp64_achieved / fp64_peak,
                           "peak_kind": f"2 FP64 instr/clk/SM x {nsm} SMs at the sampled {clk_mhz:.0f} MHz "
                                        f"(a DFMA-chain probe reaches {FP64_GOPS_MEASURED:.0f} G/s)",
+                          "frac_of_probe": fp64_achieved / FP64_GOPS_MEASURED,
                           "fp64_instr_per_component_step": opc,
                           "fp64_ops_per_component_step": alg_opc},
         "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": 8.0 * n / max(1, e2e_steps),
