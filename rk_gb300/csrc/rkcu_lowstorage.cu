@@ -31,7 +31,13 @@ __global__ void __launch_bounds__(kLsThreads) ls_kernel(const __grid_constant__ 
   __shared__ int s_acc, s_rej, s_cur, s_done, s_pending;
   __shared__ unsigned long long s_step;
   __shared__ double s_wmax[kLsThreads / 32];
-  __shared__ int s_start[kMaxStages + 1], s_stage[kMaxStages], s_nact;
+  __shared__ int s_start[kMaxStages + 1], s_stage[kMaxStages], s_blk[kMaxStages], s_nact;
+  // per active stage of a wavefront step: ring-slot bases, so that the item
+  // loop needs no division -- the stage's argument ring at blocks b-1, b, b+1,
+  // every ring at block b (the stage's writes), and the dy / err slots
+  __shared__ const double2 *s_rd[kMaxStages][3];
+  __shared__ double2 *s_wr[kMaxStages][kMaxStages];
+  __shared__ double2 *s_dyb[kMaxStages], *s_erb[kMaxStages];
 
   DevState *st = P.st;
   const int s = P.s, N = P.N, R = P.R, nb = P.nb;
@@ -87,13 +93,30 @@ __global__ void __launch_bounds__(kLsThreads) ls_kernel(const __grid_constant__ 
         s_nact = cnt;
       }
       __syncthreads();
+      if (threadIdx.x < s_nact) {
+        const int a = threadIdx.x, i = s_stage[a], b = tau - 2 * i;
+        s_blk[a] = b;
+        const int md = 2 * s - 1;
+        s_dyb[a] = P.dyring + static_cast<size_t>(b % md) * blk;
+        s_erb[a] = P.errring + static_cast<size_t>(b % md) * blk;
+        for (int l = 1; l < s; ++l)
+          s_wr[a][l] = P.ring[l] + static_cast<size_t>(b % (2 * l + 2)) * blk;
+        if (i > 0) {
+          const int m = 2 * i + 2;
+          for (int d = 0; d < 3; ++d) {
+            const int bb = b - 1 + d;  // blocks outside [0, nb) are never read
+            s_rd[a][d] = (bb >= 0 && bb < nb) ? P.ring[i] + static_cast<size_t>(bb % m) * blk : nullptr;
+          }
+        }
+      }
+      __syncthreads();
       const int nact = s_nact;
       const int total = s_start[nact];
       for (int u = gtid; u < total; u += gstride) {
         int a = 0;
         while (a + 1 < nact && u >= s_start[a + 1]) ++a;
         const int i = s_stage[a];
-        const int b = tau - 2 * i;
+        const int b = s_blk[a];
         const int q = u - s_start[a];
         const int r = static_cast<int>((static_cast<unsigned long long>(q) * P.inv_n) >> 40);
         const int j = q - r * N;
@@ -107,18 +130,21 @@ __global__ void __launch_bounds__(kLsThreads) ls_kernel(const __grid_constant__ 
           upr = ycur + static_cast<size_t>(ku) * N;
           dnr = ycur + static_cast<size_t>(kd) * N;
         } else {
-          const int m = 2 * i + 2;
-          const double2 *ring = P.ring[i];
-          const int bu = ku / R, bd = kd / R;  // R is at least 1; blocks b-1..b+1
-          cr = ring + static_cast<size_t>(b % m) * blk + static_cast<size_t>(r) * N;
-          upr = ring + static_cast<size_t>(bu % m) * blk + static_cast<size_t>(ku - bu * R) * N;
-          dnr = ring + static_cast<size_t>(bd % m) * blk + static_cast<size_t>(kd - bd * R) * N;
+          // the neighbour rows lie in blocks b-1, b or b+1
+          const double2 *const *rd = s_rd[a];
+          const int k0 = b * R;
+          cr = rd[1] + static_cast<size_t>(r) * N;
+          upr = ku < k0 ? rd[0] + static_cast<size_t>(ku - (k0 - R)) * N
+                : ku >= k0 + R ? rd[2] + static_cast<size_t>(ku - (k0 + R)) * N
+                               : rd[1] + static_cast<size_t>(ku - k0) * N;
+          dnr = kd < k0 ? rd[0] + static_cast<size_t>(kd - (k0 - R)) * N
+                : kd >= k0 + R ? rd[2] + static_cast<size_t>(kd - (k0 + R)) * N
+                               : rd[1] + static_cast<size_t>(kd - k0) * N;
         }
         const double2 F = P.bruss.eval_rows<kExact>(upr, cr, dnr, j);
         const size_t loc = static_cast<size_t>(r) * N + j;  // position inside a block slot
-        const int md = 2 * s - 1;
-        double2 *dyp = P.dyring + static_cast<size_t>(b % md) * blk + loc;
-        double2 *erp = P.errring + static_cast<size_t>(b % md) * blk + loc;
+        double2 *dyp = s_dyb[a] + loc;
+        double2 *erp = s_erb[a] + loc;
         if (i == 0) {
           const double2 Y = cr[j];
           for (int l = 1; l < s; ++l) {
@@ -128,7 +154,7 @@ __global__ void __launch_bounds__(kLsThreads) ls_kernel(const __grid_constant__ 
               wv.x = M::mac(Y.x, aa, F.x);
               wv.y = M::mac(Y.y, aa, F.y);
             }
-            P.ring[l][static_cast<size_t>(b % (2 * l + 2)) * blk + loc] = wv;
+            s_wr[a][l][loc] = wv;
           }
           *dyp = make_double2(M::mul(hb[0], F.x), M::mul(hb[0], F.y));
           *erp = make_double2(M::mul(hbh[0], F.x), M::mul(hbh[0], F.y));
@@ -146,7 +172,7 @@ __global__ void __launch_bounds__(kLsThreads) ls_kernel(const __grid_constant__ 
             for (int l = i + 1; l < s; ++l) {
               if (!P.nzA[l * kMaxStages + i]) continue;
               const double aa = hA[l * kMaxStages + i];
-              double2 *wl = P.ring[l] + static_cast<size_t>(b % (2 * l + 2)) * blk + loc;
+              double2 *wl = s_wr[a][l] + loc;
               double2 wv = *wl;
               wv.x = M::mac(wv.x, aa, F.x);
               wv.y = M::mac(wv.y, aa, F.y);
