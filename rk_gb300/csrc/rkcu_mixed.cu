@@ -284,23 +284,23 @@ __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
           if (threadIdx.x == 0) issue(blockIdx.x, 0);
           pending |= 1u;
         }
+        // A thread whose wait ran out of time skips the tile; the CTA agrees on
+        // it at the next barrier (the solve then ends with the error set).
+        bool bad = false;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x, b ^= 1) {
           const int tn = t + gridDim.x;
-          __syncthreads();  // buffer b^1 and s_delta are free
+          if (__syncthreads_or(bad)) break;  // buffer b^1 and s_delta are free
           if (tn < ntiles) {
             if (threadIdx.x == 0) issue(tn, b ^ 1);
             pending |= 2u >> b;  // bit of buffer b^1
           }
           const bool got = mbar_wait(&s_mbar[b], (phase >> b) & 1u, st, P.timeout_ns, 14);
-          if (!__syncthreads_and(got)) {
-            ok = false;
-            break;
-          }
+          bad = bad || !got;
           phase ^= 1u << b;
-          pending &= ~(1u << b);
+          if (got) pending &= ~(1u << b);
           const int k0 = (t / tiles_x) * kTileR, j0 = (t % tiles_x) * kTileC;
           const float2 *bf0 = slot(b, 0);
-          for (int hh = threadIdx.x; hh < (kTileR + 2) * (kTileC + 2); hh += blockDim.x) {
+          for (int hh = threadIdx.x; got && hh < (kTileR + 2) * (kTileC + 2); hh += blockDim.x) {
             const int hr = hh / (kTileC + 2), hcl = hh % (kTileC + 2);
             const int k = k0 + hr - 1, j = j0 + hcl - 1;
             if (k < 0 || k >= N || j < 0 || j >= N) continue;
@@ -319,13 +319,14 @@ __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
           }
           __syncthreads();
           const int k = k0 + tr, j = j0 + tc;
-          if (k < N && j < N) {
+          if (got && k < N && j < N) {
             const int eo = (tr + 1) * kBoxPairs + tc + 2;  // the point itself in a box
             finish_point(tr, tc, k, j, slot(b, 1)[eo],
                          [&](int jj) { return slot(b, 1 + jj)[eo]; },
                          [&]() { return bf0[eo]; });
           }
         }
+        if (__syncthreads_or(bad)) ok = false;
         if (!ok) break;
         fence_proxy_async_global();  // dF_i is read by TMA in later stages
       } else {
