@@ -554,7 +554,7 @@ def main():
     ap.add_argument("--sweeps-per-launch", type=int, default=256)
     ap.add_argument("--plain-sample", type=int, default=32)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--method", default="DOPRI54")
