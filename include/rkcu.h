@@ -85,9 +85,10 @@ typedef struct
                            (pass the reference's own initial_stepsize() result or H_INIT) */
   int block_rows;       /* RKCU_VARIANT_LOWSTORAGE: grid rows per pipeline block (the
                            reference's BLOCKSIZE in rows, config.h:97-98); 0 = automatic */
-  int schedule;         /* plain form, stage synchronisation: 0 = automatic, 1 = grid
-                           barrier after every stage, 2 = neighbour progress flags,
-                           3 = dataflow over (stage, tile) in wavefront order */
+  int schedule;         /* plain form, stage synchronisation: 0 = automatic (neighbour
+                           flags), 1 = grid barrier after every stage, 2 = neighbour
+                           progress flags, 3 = dataflow over (stage, tile) in wavefront
+                           order; mixed form: 1 = tiles with plain loads, else TMA */
   int flow_skew;        /* schedule 3: tiles by which stage i trails stage i-1 in the
                            wavefront; 0 = automatic (tiles are block_rows grid rows) */
 } rkcu_options;

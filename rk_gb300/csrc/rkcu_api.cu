@@ -558,9 +558,11 @@ int rkcu_advance(rkcu_solver *s, int max_steps) {
   p.err = s->stage + (size_t)s->s * s->npairs;
   p.st = s->st;
   p.flags = s->flags;
-  p.schedule = s->opt.schedule == 2   ? rkcu::kScheduleNeighbour
+  // automatic (0): neighbour progress flags, measured faster than a grid
+  // barrier after every stage at every size tried
+  p.schedule = s->opt.schedule == 1   ? rkcu::kScheduleGrid
                : s->opt.schedule == 3 ? rkcu::kScheduleFlow
-                                      : rkcu::kScheduleGrid;
+                                      : rkcu::kScheduleNeighbour;
   flow_geometry(s, &p.flow_tile, &p.flow_ntiles, &p.flow_dep);
   p.flow_skew = s->opt.flow_skew;  // 0: chosen at launch from the grid size
   // the flow schedule's tile counters hold step * s + stage within a launch
