@@ -55,7 +55,7 @@ FP64_PER_SM_CLK = 2.0
 # (dram__bytes_read.sum + dram__bytes_write.sum) at N=2000, DOPRI5(4); all
 # vectors exceed L2 at that size and above, so the figure scales with n.
 MEASURED_TRAFFIC = {
-    ("d", "exact", "DOPRI54"): (480.0, "one-pass ncu capture of the timed launches of this benchmark at N=2000"),
+    ("d", "exact", "DOPRI54"): (569.0, "one-pass ncu capture of the timed launches of this benchmark at N=2000"),
     ("d", "mixed", "DOPRI54"): (163.0, "ncu --set full of a 3-step launch at N=2000, scaled by n"),
 }
 
