@@ -73,7 +73,8 @@ def fp64_ops_per_comp(method, precision):
     exact mode the products run on the integer pipes (software binary64
     multiply), so the FP64 pipe executes the sums only (about 7.3 per
     right-hand side with its max/compare work).  The mixed form keeps only F0
-    (7.5), the FP64 update (2) and two conversions."""
+    (8.5 operations, of which the plain products run in software) and the FP64
+    update (2); its conversions to float run on the integer pipe."""
     if precision == "mixed":
         return 10.0, 12.0
     import rk_gb300 as rk
