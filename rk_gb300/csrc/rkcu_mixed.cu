@@ -3,8 +3,13 @@
 //
 // On GB300 the FP64 pipe (and every FP64<->FP32 conversion) runs at 1/72 of
 // the FP32 rate, so the FP32 stages must avoid both.  Per step and component:
-//   F0 = f(y)                          FP64 (fused), once per step
-//   y1 = y + (h * sum b) * F0           FP64, the large part of the update
+//   F0 = f(y)                          double-float, once per step: the
+//                                       Laplacian exact in 64-bit fixed point
+//                                       on the integer pipe, the rest in FP32
+//                                       pairs (about 2^-46 relative), FP64 only
+//                                       where a value leaves those ranges
+//   y1 = y + (h * sum b) * F0           FP64 sums of y and the double-float
+//                                       product, the large part of the update
 //   stage i >= 1:  delta_i = h c_i F0 + sum_{1<=j<i} h a_ij dF_j                (FP32)
 //                  dF_i = f(y + delta_i) - F0 = alpha (N-1)^2 lap(delta_i)
 //                         + [u^2 v](y + delta) - [u^2 v](y) -/+ 4.4 du / 3.4 du  (FP32)
@@ -15,8 +20,9 @@
 //   y_new = y1 + dY                     FP64
 //   err max = max |e| / max(|y_new|, |y_old|): per thread in FP32, reduced in FP64
 // c_i is taken as the row sum of A (sum_j a_ij), so sum_j h a_ij F0 = h c_i F0.
-// FP64 instructions per component-step: about 12 (RHS 7.5, update 2, two
-// conversions) instead of 85-128 for the FP64 forms.
+// FP64 instructions per component-step: 3 (the sums of the update; the
+// conversions between float and double are built from bit fields) instead of
+// 85-128 for the FP64 forms.
 //
 // Memory: this form is bound by HBM traffic, not arithmetic, so it stores each
 // stage's dF_i once and gathers delta_i from dF_1 .. dF_{i-1} at the five
@@ -29,6 +35,7 @@
 #include <cudaTypedefs.h>  // PFN_cuTensorMapEncodeTiled
 
 #include "rkcu.h"
+#include "rkcu_dfloat.cuh"
 #include "rkcu_mixed.cuh"
 #include "rkcu_tma.cuh"
 
@@ -107,6 +114,19 @@ __device__ __forceinline__ float2 delta_at(const float2 *const *jp, const float 
   return make_float2(fmaf(hc, f.x, acc.x), fmaf(hc, f.y, acc.y));
 }
 
+// Stage 0 at one pair in FP64 (fused, products in software binary64): the
+// path for points whose values the double-float evaluation does not cover.
+// Out of line, so that its FP64 instructions are not if-converted into the
+// double-float loop.
+static __device__ __noinline__ void stage0_point_fp64(const Bruss &br, const double2 *__restrict__ ycur, int p,
+                                                      double hbs, double2 *__restrict__ ynew,
+                                                      float2 *__restrict__ f0) {
+  const double2 F = br.eval<kArithFusedSoftMul>(ycur, p);
+  const double2 Y = ycur[p];
+  ynew[p] = make_double2(fma(hbs, F.x, Y.x), fma(hbs, F.y, Y.y));
+  f0[p] = make_float2(softfp::to_float(F.x), softfp::to_float(F.y));
+}
+
 // kMaxS: an upper bound of the stage count (8 or 13), so that the per-stage
 // loops over earlier stages unroll; kPath: how the FP32 stages walk the grid.
 template <int kMaxS, int kPath>
@@ -129,6 +149,7 @@ __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
   __shared__ float s_ja[kMaxStages][kMaxStages];
   __shared__ int s_nj[kMaxStages];
   __shared__ double s_hbsum;
+  __shared__ float s_hbs_hi, s_hbs_lo;  // h sum(b) as a double-float pair
   __shared__ float s_hbhsum;
   __shared__ float2 s_delta[kTileR + 2][kTileC + 2];  // delta_i on a tile and its halo
 
@@ -139,6 +160,7 @@ __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const Bruss &br = P.bruss;
   const float coef = static_cast<float>(br.coef);
+  const dfl::df coef_df = {coef, static_cast<float>(br.coef - static_cast<double>(coef))};
 
   if (threadIdx.x == 0) {
     s_t = st->t;
@@ -181,23 +203,45 @@ __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
     }
     if (threadIdx.x == 0) {
       s_hbsum = h * P.bsum;
+      s_hbs_hi = static_cast<float>(s_hbsum);
+      s_hbs_lo = static_cast<float>(s_hbsum - static_cast<double>(s_hbs_hi));
       s_hbhsum = static_cast<float>(h * P.bhsum);
     }
     __syncthreads();
     const double2 *__restrict__ ycur = P.y[s_cur];
     double2 *__restrict__ ynew = P.y[s_cur ^ 1];
 
-    // stage 0: F0 = f(y) in FP64, y1 = y + h sum(b) F0, F0 and y rounded to FP32
+    // stage 0: F0 = f(y) in double-float (fixed-point Laplacian, FP32 pairs),
+    // y1 = y + h sum(b) F0 in FP64, F0 and y rounded to FP32; a point whose
+    // values fall outside the double-float ranges takes the FP64 evaluation
     {
-      const double hbs = s_hbsum;
-      for (int p = gtid; p < P.npairs; p += gstride) {
-        const double2 F = br.eval<kArithFusedSoftMul>(ycur, p);
-        const double2 Y = ycur[p];
-        ynew[p] = make_double2(fma(hbs, F.x, Y.x), fma(hbs, F.y, Y.y));
-        // rounded to float on the integer pipe (the conversion instruction would
-        // use the FP64 pipe, this stage's bottleneck)
-        P.f0[p] = make_float2(softfp::to_float(F.x), softfp::to_float(F.y));
-        P.y32[p] = make_float2(trunc_to_float(Y.x), trunc_to_float(Y.y));
+      const dfl::df hbd = {s_hbs_hi, s_hbs_lo};
+      const int N = br.N;
+      // grid point (k, j) of pair p, advanced by the grid stride without a division
+      const int dk = gstride / N, dj = gstride - dk * N;
+      int k = gtid / N, j = gtid - (gtid / N) * N;
+      for (int p = gtid; p < P.npairs; p += gstride, j += dj, k += dk) {
+        if (j >= N) {
+          j -= N;
+          ++k;
+        }
+        const double2 *row = ycur + (p - j);
+        const double2 c = row[j];
+        const double2 up = (k == 0 ? row + N : row - N)[j];
+        const double2 dn = (k == N - 1 ? row - N : row + N)[j];
+        // a boundary column passes its inner neighbour twice
+        const double2 w = row[j == 0 ? 1 : j - 1];
+        const double2 e = row[j == N - 1 ? j - 1 : j + 1];
+        dfl::df fu, fv;
+        if (dfl::bruss_rhs_df(c, up, dn, w, e, coef_df, &fu, &fv)) {
+          const dfl::df qu = dfl::df_mul(hbd, fu), qv = dfl::df_mul(hbd, fv);
+          ynew[p] = make_double2(__dadd_rn(__dadd_rn(c.x, dfl::dbl_of(qu.hi)), dfl::dbl_of(qu.lo)),
+                                 __dadd_rn(__dadd_rn(c.y, dfl::dbl_of(qv.hi)), dfl::dbl_of(qv.lo)));
+          P.f0[p] = make_float2(fu.hi, fv.hi);
+        } else {
+          stage0_point_fp64(br, ycur, p, s_hbsum, ynew, P.f0);
+        }
+        P.y32[p] = make_float2(trunc_to_float(c.x), trunc_to_float(c.y));
       }
     }
     if (kPath == kMixTilesTma) fence_proxy_async_global();  // f0, y32 are read by TMA next
@@ -246,8 +290,8 @@ __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
           er.y = fmaf(hbh[jj], d.y, er.y);
         }
         const double2 y1 = ynew[p];
-        const double2 yn = make_double2(y1.x + static_cast<double>(sum.x - cmp.x),
-                                        y1.y + static_cast<double>(sum.y - cmp.y));
+        const double2 yn = make_double2(__dadd_rn(y1.x, dfl::dbl_of(sum.x - cmp.x)),
+                                        __dadd_rn(y1.y, dfl::dbl_of(sum.y - cmp.y)));
         ynew[p] = yn;
         const float dnx = fmaxf(fabsf(trunc_to_float(yn.x)), fabsf(y32.x));
         const float dny = fmaxf(fabsf(trunc_to_float(yn.y)), fabsf(y32.y));

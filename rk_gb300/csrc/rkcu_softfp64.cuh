@@ -97,6 +97,14 @@ inline float hw_to_float(double x) {
 #endif
 }
 
+#ifdef __CUDACC__
+static __host__ __device__ __noinline__ double hw_to_double(float x) {
+#else
+inline double hw_to_double(float x) {
+#endif
+  return static_cast<double>(x);
+}
+
 SFP_HD float float_of(uint32_t b) {
 #ifdef __CUDA_ARCH__
   return __uint_as_float(b);
