@@ -107,6 +107,21 @@ struct Arith<kArithFused> {
 // reference sums "yN + yS" first (a boundary row doubles the inner neighbour,
 // which "y + y" reproduces exactly), then adds W and E left to right in
 // interior columns, or "2 * inner" in one rounding in the first/last column.
+// The BRUSS2D-MIX Laplacian on the FP64 pipe in the order of
+// src/problems/bruss2d-mix.c (see Bruss::eval_rows); out of line, so that the
+// integer path's callers do not get it if-converted into every lane.
+static __device__ __noinline__ double2 lap2_fp64(double2 n, double2 s, double2 w, double2 e, double2 c,
+                                                  int jcase) {
+  double2 l = make_double2(__dadd_rn(n.x, s.x), __dadd_rn(n.y, s.y));
+  if (jcase == 0) {
+    l = make_double2(__dadd_rn(__dadd_rn(l.x, w.x), e.x), __dadd_rn(__dadd_rn(l.y, w.y), e.y));
+  } else {
+    const double2 t = jcase == 1 ? e : w;
+    l = make_double2(__fma_rn(2.0, t.x, l.x), __fma_rn(2.0, t.y, l.y));
+  }
+  return make_double2(__fma_rn(-4.0, c.x, l.x), __fma_rn(-4.0, c.y, l.y));
+}
+
 struct Bruss {
   int N;        // grid size
   double coef;  // (alpha * (N-1)) * (N-1), evaluated on the host in that order
@@ -132,26 +147,22 @@ struct Bruss {
     const double2 c = cr[j];
     const double2 up = upr[j];
     const double2 dn = dnr[j];
-    const double2 *w = cr;
-    const int p = j;
-    double lu = M::add(up.x, dn.x);
-    double lv = M::add(up.y, dn.y);
-    if (j == 0) {
-      const double2 e = w[p + 1];
-      lu = fma(2.0, e.x, lu);
-      lv = fma(2.0, e.y, lv);
-    } else if (j == N - 1) {
-      const double2 ww = w[p - 1];
-      lu = fma(2.0, ww.x, lu);
-      lv = fma(2.0, ww.y, lv);
-    } else {
-      const double2 ww = w[p - 1];
-      const double2 e = w[p + 1];
-      lu = M::add(M::add(lu, ww.x), e.x);
-      lv = M::add(M::add(lv, ww.y), e.y);
+    // jcase 1: first column (the east neighbour twice), 2: last column (the
+    // west one twice), 0: interior
+    const int jcase = j == 0 ? 1 : (j == N - 1 ? 2 : 0);
+    const double2 ww = cr[jcase == 1 ? j + 1 : j - 1];
+    const double2 e = cr[jcase == 2 ? j - 1 : j + 1];
+    // ((up + dn) + w) + e - 4c, or (up + dn) + 2t - 4c at a boundary column,
+    // each operation rounded: in integer arithmetic where the five values share
+    // a binade (bit-identical), else on the FP64 pipe
+    double lu = 0.0, lv = 0.0;
+    const bool fast = softfp::lap_same_binade(up.x, dn.x, ww.x, e.x, c.x, jcase, &lu) &
+                      softfp::lap_same_binade(up.y, dn.y, ww.y, e.y, c.y, jcase, &lv);
+    if (!fast) {
+      const double2 l = lap2_fp64(up, dn, ww, e, c, jcase);
+      lu = l.x;
+      lv = l.y;
     }
-    lu = fma(-4.0, c.x, lu);
-    lv = fma(-4.0, c.y, lv);
     const double u2v = M::mul(M::mul(c.x, c.x), c.y);  // shared by U and V
     const double ru = M::submul(M::add(1.0, u2v), 4.4, c.x);
     const double rv = M::msub(3.4, c.x, u2v);

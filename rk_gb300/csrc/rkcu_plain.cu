@@ -43,7 +43,7 @@ __device__ __forceinline__ bool stage_sync(const PlainParams &P, int c_lo, int c
 }
 
 template <class Prob, int kExact>
-__global__ void __launch_bounds__(kThreads) plain_kernel(const __grid_constant__ PlainParams P) {
+__global__ void __launch_bounds__(kThreads, 4) plain_kernel(const __grid_constant__ PlainParams P) {
   using M = Arith<kExact>;
   __shared__ double hA[kMaxStages * kMaxStages];
   __shared__ double hb[kMaxStages], hbh[kMaxStages];

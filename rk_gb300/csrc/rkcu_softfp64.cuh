@@ -207,5 +207,54 @@ SFP_HD double add(double a, double b) {
   return double_of(sign | ((static_cast<uint64_t>(e - 1) << 52) + m));
 }
 
+// s rounded to a multiple of 2^k (k = 1, 2), ties to an even multiple of 2^k:
+// the rounding of a sum of same-binade significands to the binade above.
+SFP_HD uint64_t round_units(uint64_t s, int k) {
+  const uint64_t q = s >> k, r = s & ((1ull << k) - 1u), half = 1ull << (k - 1);
+  return (q + static_cast<uint64_t>((r > half) | ((r == half) & ((q & 1u) != 0u)))) << k;
+}
+
+// The five-point Laplacian of BRUSS2D-MIX in the order of its FP64 code,
+//   interior (jcase 0):        ((n + s) + w) + e - 4 c
+//   first/last column (1, 2):  (n + s) + 2 t - 4 c      (t = the inner neighbour)
+// each operation rounded to nearest even, computed exactly in 64-bit integers
+// when all operands have one sign and one exponent field (a resolved field):
+// the significands then share one unit, n + s rounds to the binade above, the
+// next sum to the binade above that or the one after, and the final difference
+// is exact (Sterbenz: both operands lie in [2^54, 2^55] units).  Returns
+// false, leaving *out unset, for any other operands.
+SFP_HD bool lap_same_binade(double n, double s, double w, double e, double c, int jcase, double *out) {
+  const uint64_t bn = bits_of(n), bs = bits_of(s), bw = bits_of(w), be = bits_of(e), bc = bits_of(c);
+  const uint32_t top = static_cast<uint32_t>(bc >> 52);  // sign and exponent field
+  const uint32_t ef = top & 0x7ffu;
+  if (static_cast<uint32_t>(bn >> 52) != top || static_cast<uint32_t>(bs >> 52) != top ||
+      static_cast<uint32_t>(bw >> 52) != top || static_cast<uint32_t>(be >> 52) != top || ef == 0u || ef > 2043u)
+    return false;  // (the partial sums reach three binades up: no overflow below 2044)
+  constexpr uint64_t kF = 0x000fffffffffffffull, kH = 0x0010000000000000ull;
+  const uint64_t r1 = round_units(((bn & kF) | kH) + ((bs & kF) | kH), 1);  // in [2^53, 2^54]
+  uint64_t r;
+  if (jcase == 0) {
+    const uint64_t s2 = r1 + ((bw & kF) | kH);                  // in [3 2^52, 3 2^53)
+    const uint64_t r2 = round_units(s2, s2 >= (1ull << 54) ? 2 : 1);
+    r = round_units(r2 + ((be & kF) | kH), 2);                   // in [2^54, 2^55]
+  } else {
+    const uint64_t t = jcase == 1 ? be : bw;
+    r = round_units(r1 + (((t & kF) | kH) << 1), 2);              // in [2^54, 2^55]
+  }
+  const int64_t L = static_cast<int64_t>(r) - static_cast<int64_t>(((bc & kF) | kH) << 2);  // exact
+  if (L == 0) {
+    *out = 0.0;  // x - x is +0 in round to nearest
+    return true;
+  }
+  const uint64_t a = L < 0 ? static_cast<uint64_t>(-L) : static_cast<uint64_t>(L);  // a multiple of 4, <= 2^54
+  const int p = 63 - clz64(a);                     // value = a 2^(ef - 1075) = 1.f 2^(p + ef - 1075)
+  const int f = p + static_cast<int>(ef) - 52;     // biased exponent of the result
+  if (f < 1) return false;                          // subnormal: not on this path
+  const uint64_t m = p >= 52 ? (a >> (p - 52)) : (a << (52 - p));  // exact: a's low 2 bits are 0
+  const uint64_t sign = (static_cast<uint64_t>(top & 0x800u) << 52) ^ (L < 0 ? 0x8000000000000000ull : 0ull);
+  *out = double_of(sign | ((static_cast<uint64_t>(f - 1) << 52) + m));
+  return true;
+}
+
 }  // namespace softfp
 }  // namespace rkcu

@@ -2,6 +2,7 @@
 // against the host's IEEE round-to-nearest arithmetic.  Compiled with
 // -ffp-contract=off.  Usage: softfp64_check <count> <seed>; prints mismatches.
 #include <cinttypes>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -74,5 +75,49 @@ int main(int argc, char **argv) {
     }
   }
   printf("mismatches mul %lld add %lld to_float %lld of %lld\n", bad_mul, bad_add, bad_cvt, count);
-  return (bad_mul || bad_add || bad_cvt) ? 1 : 0;
+
+  // the same-binade Laplacian against the FP64 sequence it replaces: operands
+  // of one exponent field (random significands, significands near the top of
+  // the binade, few-bit significands for ties), both signs, all three forms;
+  // and operands of different binades, which it must refuse
+  long long bad_lap = 0, taken = 0;
+  for (long long i = 0; i < count; ++i) {
+    const uint64_t r = next();
+    const uint64_t ef = 1 + (r >> 11) % 2046;
+    const uint64_t sg = (r >> 63) << 63;
+    double v[5];
+    for (int k = 0; k < 5; ++k) {
+      const uint64_t q = next();
+      uint64_t f;
+      switch ((r >> (2 * k)) & 3) {
+        case 0: f = q & 0x000fffffffffffffull; break;
+        case 1: f = 0x000fffffffffffffull - (q & 0xff); break;               // near the top
+        case 2: f = (q & 0xf) << ((q >> 8) % 49); break;                      // few bits: ties
+        default: f = (q & 0x000fffffffffffffull) | 0x000ffffff0000000ull; break;
+      }
+      v[k] = double_of(sg | (ef << 52) | f);
+    }
+    if ((r >> 20) % 8 == 0) v[(r >> 24) % 5] = draw(2, 0.0);  // a different binade (usually)
+    const int jcase = static_cast<int>((r >> 30) % 3);
+    const double n = v[0], sv = v[1], w = jcase == 1 ? v[3] : v[2], e = jcase == 2 ? v[2] : v[3], c = v[4];
+    double want = n + sv;
+    if (jcase == 0)
+      want = (want + w) + e;
+    else
+      want = std::fma(2.0, jcase == 1 ? e : w, want);
+    want = std::fma(-4.0, c, want);
+    double got = 0.0;
+    const bool same = (bits_of(n) >> 52) == (bits_of(c) >> 52) && (bits_of(sv) >> 52) == (bits_of(c) >> 52) &&
+                      (bits_of(w) >> 52) == (bits_of(c) >> 52) && (bits_of(e) >> 52) == (bits_of(c) >> 52) &&
+                      ef <= 2043;
+    const bool ok = rkcu::softfp::lap_same_binade(n, sv, w, e, c, jcase, &got);
+    if (ok) ++taken;
+    const bool sub = (bits_of(want) & 0x7ff0000000000000ull) == 0;  // subnormal or zero results may refuse
+    if ((ok && bits_of(got) != bits_of(want) && want == want) || (ok && !same) || (!ok && same && !sub && want == want &&
+                                                                                   std::fabs(want) < 1e300)) {
+      if (bad_lap++ < 5) printf("lap %d: %a %a %a %a %a: fp64 %a int %a (ok %d)\n", jcase, n, sv, w, e, c, want, got, ok);
+    }
+  }
+  printf("lap mismatches %lld (fast path taken %lld of %lld)\n", bad_lap, taken, count);
+  return (bad_mul || bad_add || bad_cvt || bad_lap) ? 1 : 0;
 }
