@@ -69,13 +69,16 @@ def fp64_ops_per_comp(method, precision):
     BRUSS2D-MIX step loop, counted from the kernel.  Operations: a right-hand
     side costs 9.5 (exact: 6.5 sums + 3 products) / 7.5 (fused) per component,
     each nonzero tableau coefficient a product and a sum (exact) or one FMA,
-    the update one sum, the error norm about 0.5 after its filter.  In the
-    exact mode the products run on the integer pipes (software binary64
-    multiply), so the FP64 pipe executes the sums only (about 7.3 per
-    right-hand side with its max/compare work).  The mixed form evaluates F0
-    in double-float arithmetic (FP32 pairs, the Laplacian in integer fixed
-    point) and keeps three FP64 sums per component-step: y + (h sum b F0) as
-    two sums, and y1 + dY; its conversions run on the integer pipe."""
+    the update one sum, the error norm about 0.5 after its filter.  On the FP64
+    pipe: the Laplacian's four sums run on the integer pipe (exact integer
+    arithmetic where the five values share a binade, which is nearly every
+    point), so a right-hand side keeps 2.5 sums per component; in the exact
+    mode its 3 products per component run on the FP64 pipe (with max/compare
+    work 6.3 per right-hand side) while the tableau products run in software
+    binary64 on the integer pipe; the fused mode keeps 3.5 per right-hand side.
+    The mixed form evaluates F0 in double-float arithmetic (FP32 pairs, the
+    Laplacian in integer fixed point) and keeps three FP64 sums per
+    component-step: y + (h sum b F0) as two sums, and y1 + dY."""
     if precision == "mixed":
         return 3.0, 3.0
     import rk_gb300 as rk
@@ -87,10 +90,10 @@ def fp64_ops_per_comp(method, precision):
     if precision.startswith("exact"):
         ops = 9.5 * s + 2 * nz_a + (2 * nz_b - 1) + (2 * nz_bh - 1) + 1.5
         if precision == "exact-hwmul":
-            return ops, ops
-        return 7.3 * s + nz_a + (nz_b - 1) + (nz_bh - 1) + 1.5, ops
+            return 5.5 * s + 2 * nz_a + (2 * nz_b - 1) + (2 * nz_bh - 1) + 1.5, ops
+        return 6.3 * s + nz_a + (nz_b - 1) + (nz_bh - 1) + 1.5, ops
     ops = 7.5 * s + nz_a + nz_b + nz_bh + 1.5
-    return ops, ops
+    return 3.5 * s + nz_a + nz_b + nz_bh + 1.5, ops
 
 
 def _peaks():

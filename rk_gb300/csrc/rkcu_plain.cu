@@ -17,6 +17,8 @@
 // last stage before the error max is read.  The error max is reduced by warp
 // shuffles, shared memory and one 64-bit atomicMax per CTA on the bit pattern
 // (the values are >= 0).
+#include <type_traits>
+
 #include "rkcu_plain.cuh"
 #include "rkcu.h"
 
@@ -42,9 +44,24 @@ __device__ __forceinline__ bool stage_sync(const PlainParams &P, int c_lo, int c
   return wait_neighbours(P.flags, c_lo, c_hi, progress, P.st, P.timeout_ns, site);
 }
 
+// Resident CTAs per SM (the register budget) and the arithmetic of the
+// right-hand side, per mode, as measured on BRUSS2D-MIX at N=2000 (all bit-identical): with
+// the Laplacian on the integer pipe, the exact mode is fastest with the
+// right-hand side's products on the FP64 pipe (the tableau products stay in
+// software) at 5 CTAs, the fused mode with all plain products in software at 6.
 template <class Prob, int kExact>
-__global__ void __launch_bounds__(kThreads, 4) plain_kernel(const __grid_constant__ PlainParams P) {
+constexpr int plain_min_blocks() {
+  return !std::is_same<Prob, Bruss>::value ? 4 : kExact == kArithFusedSoftMul ? 6 : kExact == kArithExactSoftMul ? 5 : 4;
+}
+template <int kExact>
+constexpr int plain_rhs_mode() {
+  return kExact == kArithExactSoftMul ? kArithExact : kExact;
+}
+
+template <class Prob, int kExact>
+__global__ void __launch_bounds__(kThreads, plain_min_blocks<Prob, kExact>()) plain_kernel(const __grid_constant__ PlainParams P) {
   using M = Arith<kExact>;
+  constexpr int kRhs = plain_rhs_mode<kExact>();
   __shared__ double hA[kMaxStages * kMaxStages];
   __shared__ double hb[kMaxStages], hbh[kMaxStages];
   __shared__ double s_t, s_h;
@@ -110,7 +127,7 @@ __global__ void __launch_bounds__(kThreads, 4) plain_kernel(const __grid_constan
 
     // first stage at pair p (block-inline.h:253-272)
     auto stage_first = [&](int p) {
-      const double2 F = prob.template eval<kExact>(ycur, p);
+      const double2 F = prob.template eval<kRhs>(ycur, p);
       const double2 Y = ycur[p];
       for (int l = 1; l < s; ++l) {
         double2 wv = Y;
@@ -126,7 +143,7 @@ __global__ void __launch_bounds__(kThreads, 4) plain_kernel(const __grid_constan
     };
     // intermediate stage i at pair p (block-inline.h:276-294)
     auto stage_mid = [&](int i, int p) {
-      const double2 F = prob.template eval<kExact>(P.w[i], p);
+      const double2 F = prob.template eval<kRhs>(P.w[i], p);
       for (int l = i + 1; l < s; ++l) {
         if (!P.nzA[l * kMaxStages + i]) continue;
         const double a = hA[l * kMaxStages + i];
@@ -154,7 +171,7 @@ __global__ void __launch_bounds__(kThreads, 4) plain_kernel(const __grid_constan
     ErrMax em;
     auto stage_last = [&](int p) {
       const int i = s - 1;
-      const double2 F = prob.template eval<kExact>(P.w[i], p);
+      const double2 F = prob.template eval<kRhs>(P.w[i], p);
       double2 d = P.dy[p];
       double2 e = P.err[p];
       if (P.nzb[i]) {
