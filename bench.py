@@ -500,14 +500,14 @@ def run_served(args):
 
     reqs = workloads.served_requests(20000, seed=7)[: args.requests]
     # capacity estimate: component-steps of the sample at the batched rate measured
-    # on this part (4.7e9 component-steps/s in the FP64 exact mode, 1024 instances)
+    # on this part (5.3e9 component-steps/s in the FP64 exact mode, 1024 instances)
     work = 0.0
     for r in reqs:
         if r["kind"] == "bruss":
             work += workloads.estimated_work(dict(grid_n=r["grid_n"], alpha=2e-3))
         else:
             work += r["n"] * 40.0
-    busy = work / 4.7e9
+    busy = work / 5.3e9
     span = reqs[-1]["arrival"]
     scale = busy / (args.load * span)
     loop = serving.ServingLoop(int(args.arena_gb * (1 << 30)), max_instances=4096,

@@ -23,8 +23,12 @@ namespace rkcu {
 constexpr int kLsThreads = 256;
 
 template <int kExact>
-__global__ void __launch_bounds__(kLsThreads) ls_kernel(const __grid_constant__ LsParams P) {
+__global__ void __launch_bounds__(kLsThreads, 4) ls_kernel(const __grid_constant__ LsParams P) {
   using M = Arith<kExact>;
+  // the right-hand side's products on the FP64 pipe in the exact mode (its
+  // Laplacian runs on the integer pipe, the tableau products in software):
+  // measured faster, same bits
+  constexpr int kRhs = kExact == kArithExactSoftMul ? kArithExact : kExact;
   __shared__ double hA[kMaxStages * kMaxStages];
   __shared__ double hb[kMaxStages], hbh[kMaxStages];
   __shared__ double s_t, s_h, s_pend_err, s_pend_h;
@@ -141,7 +145,7 @@ __global__ void __launch_bounds__(kLsThreads) ls_kernel(const __grid_constant__ 
                 : kd >= k0 + R ? rd[2] + static_cast<size_t>(kd - (k0 + R)) * N
                                : rd[1] + static_cast<size_t>(kd - k0) * N;
         }
-        const double2 F = P.bruss.eval_rows<kExact>(upr, cr, dnr, j);
+        const double2 F = P.bruss.eval_rows<kRhs>(upr, cr, dnr, j);
         const size_t loc = static_cast<size_t>(r) * N + j;  // position inside a block slot
         double2 *dyp = s_dyb[a] + loc;
         double2 *erp = s_erb[a] + loc;
