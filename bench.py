@@ -55,8 +55,9 @@ FP64_PER_SM_CLK = 2.0
 # (dram__bytes_read.sum + dram__bytes_write.sum) at N=2000, DOPRI5(4); all
 # vectors exceed L2 at that size and above, so the figure scales with n.
 MEASURED_TRAFFIC = {
-    ("d", "exact", "DOPRI54"): (569.0, "one-pass ncu capture of the timed launches of this benchmark at N=2000"),
-    ("d", "mixed", "DOPRI54"): (163.0, "ncu --set full of a 3-step launch at N=2000, scaled by n"),
+    ("d", "exact", "DOPRI54"): (553.0, "one-pass ncu capture of the timed launches of this benchmark at N=2000"),
+    ("d", "fma", "DOPRI54"): (573.0, "ncu --set full of a 3-step launch at N=2000"),
+    ("d", "mixed", "DOPRI54"): (164.0, "ncu --set full of a 3-step launch at N=2000, scaled by n"),
 }
 
 KERNEL_NAME = {"d": "plain_kernel (persistent, all stages of K steps)",
