@@ -34,6 +34,8 @@
 // (f0, y32, dF_1 .. dF_{s-2}) instead of s + 3.
 #include <cudaTypedefs.h>  // PFN_cuTensorMapEncodeTiled
 
+#include <type_traits>
+
 #include "rkcu.h"
 #include "rkcu_dfloat.cuh"
 #include "rkcu_mixed.cuh"
@@ -261,7 +263,7 @@ __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
       // dF_i (and, in the last stage, dY, e and y_new) at grid point p from
       // delta_i on the tile (s_delta), y32, and the point's own dF_j / f0
       auto finish_point_at = [&](int p, int k, int j, float2 c, float2 up, float2 dn, float2 w,
-                                 float2 e, float2 y32, auto &&own_dF, auto &&own_f0) {
+                                 float2 e, float2 y32, auto &&own_dF, auto &&own_f0, auto &&own_y1) {
         const int jcase = j == 0 ? 1 : (j == N - 1 ? 2 : 0);
         const float2 dF = delta_rhs(c, up, dn, w, e, jcase, y32, coef);
         if (!last) {
@@ -289,7 +291,7 @@ __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
           er.x = fmaf(hbh[jj], d.x, er.x);
           er.y = fmaf(hbh[jj], d.y, er.y);
         }
-        const double2 y1 = ynew[p];
+        const double2 y1 = own_y1();
         const double2 yn = make_double2(__dadd_rn(y1.x, dfl::dbl_of(sum.x - cmp.x)),
                                         __dadd_rn(y1.y, dfl::dbl_of(sum.y - cmp.y)));
         ynew[p] = yn;
@@ -299,11 +301,11 @@ __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
         if (2 * p + 1 < P.n) emax = fmaxf(emax, dny == 0.0f ? 3.0e38f : fabsf(er.y) / dny);
       };
       auto finish_point = [&](int tr_, int tc_, int k, int j, float2 y32, auto &&own_dF,
-                              auto &&own_f0) {
+                              auto &&own_f0, auto &&own_y1) {
         finish_point_at(k * N + j, k, j, s_delta[tr_ + 1][tc_ + 1],
                         s_delta[k == 0 ? tr_ + 2 : tr_][tc_ + 1],
                         s_delta[k == N - 1 ? tr_ : tr_ + 2][tc_ + 1], s_delta[tr_ + 1][tc_],
-                        s_delta[tr_ + 1][tc_ + 2], y32, own_dF, own_f0);
+                        s_delta[tr_ + 1][tc_ + 2], y32, own_dF, own_f0, own_y1);
       };
 
       if constexpr (kPath == kMixTilesTma) {
@@ -338,28 +340,42 @@ __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
             if (threadIdx.x == 0) issue(tn, b ^ 1);
             pending |= 2u >> b;  // bit of buffer b^1
           }
+          const int k0 = (t / tiles_x) * kTileR, j0 = (t % tiles_x) * kTileC;
           const bool got = mbar_wait(&s_mbar[b], (phase >> b) & 1u, st, P.timeout_ns, 14);
           bad = bad || !got;
-          phase ^= 1u << b;
-          if (got) pending &= ~(1u << b);
-          const int k0 = (t / tiles_x) * kTileR, j0 = (t % tiles_x) * kTileC;
+          if (got) {  // (a wait that ran out keeps the parity, for the final wait)
+            phase ^= 1u << b;
+            pending &= ~(1u << b);
+          }
           const float2 *bf0 = slot(b, 0);
-          for (int hh = threadIdx.x; got && hh < (kTileR + 2) * (kTileC + 2); hh += blockDim.x) {
-            const int hr = hh / (kTileC + 2), hcl = hh % (kTileC + 2);
-            const int k = k0 + hr - 1, j = j0 + hcl - 1;
-            if (k < 0 || k >= N || j < 0 || j >= N) continue;
-            const int e = hr * kBoxPairs + hcl + 1;
-            float2 acc = make_float2(0.0f, 0.0f);
+          // delta_i on the tile and its halo, with the stage's term count as a
+          // compile-time constant (no predicated-off terms in the early stages)
+          auto halo = [&](auto nj_c) {
+            constexpr int kNj = decltype(nj_c)::value;
+            for (int hh = threadIdx.x; got && hh < (kTileR + 2) * (kTileC + 2); hh += blockDim.x) {
+              const int hr = hh / (kTileC + 2), hcl = hh % (kTileC + 2);
+              const int k = k0 + hr - 1, j = j0 + hcl - 1;
+              if (k < 0 || k >= N || j < 0 || j >= N) continue;
+              const int e = hr * kBoxPairs + hcl + 1;
+              float2 acc = make_float2(0.0f, 0.0f);
 #pragma unroll
-            for (int kk = 0; kk < kMaxS - 2; ++kk) {
-              if (kk < nj) {
+              for (int kk = 0; kk < kNj; ++kk) {
                 const float2 d = slot(b, 1 + s_jl[i][kk])[e];
                 acc.x = fmaf(ja[kk], d.x, acc.x);
                 acc.y = fmaf(ja[kk], d.y, acc.y);
               }
+              const float2 f = bf0[e];
+              s_delta[hr][hcl] = make_float2(fmaf(hci, f.x, acc.x), fmaf(hci, f.y, acc.y));
             }
-            const float2 f = bf0[e];
-            s_delta[hr][hcl] = make_float2(fmaf(hci, f.x, acc.x), fmaf(hci, f.y, acc.y));
+          };
+          switch (nj) {
+            case 0: halo(std::integral_constant<int, 0>{}); break;
+            case 1: halo(std::integral_constant<int, 1>{}); break;
+            case 2: halo(std::integral_constant<int, 2>{}); break;
+            case 3: halo(std::integral_constant<int, 3>{}); break;
+            case 4: halo(std::integral_constant<int, 4>{}); break;
+            case 5: halo(std::integral_constant<int, 5>{}); break;
+            default: halo(std::integral_constant<int, (kMaxS - 2 > 6 ? 6 : kMaxS - 2)>{}); break;
           }
           __syncthreads();
           const int k = k0 + tr, j = j0 + tc;
@@ -367,7 +383,7 @@ __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
             const int eo = (tr + 1) * kBoxPairs + tc + 2;  // the point itself in a box
             finish_point(tr, tc, k, j, slot(b, 1)[eo],
                          [&](int jj) { return slot(b, 1 + jj)[eo]; },
-                         [&]() { return bf0[eo]; });
+                         [&]() { return bf0[eo]; }, [&]() { return ynew[k * N + j]; });
           }
         }
         if (__syncthreads_or(bad)) ok = false;
@@ -390,7 +406,7 @@ __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
           if (k >= N || j >= N) continue;
           const int p = k * N + j;
           finish_point(tr, tc, k, j, P.y32[p], [&](int jj) { return P.dF[jj][p]; },
-                       [&]() { return P.f0[p]; });
+                       [&]() { return P.f0[p]; }, [&]() { return ynew[p]; });
         }
       }
       if (!last) {
