@@ -1,6 +1,7 @@
-// Device check of the software binary64 multiply/add and double -> float
-// rounding (rkcu_softfp64.cuh) against the FP64 pipe's __dmul_rn/__dadd_rn/
-// __double2float_rn on random and adversarial operands.  Usage: softfp64_check_gpu <count> <seed>; prints mismatches.
+// Device check of the software binary64 multiply/add, double -> float
+// rounding and the same-binade Laplacian (rkcu_softfp64.cuh) against the FP64
+// pipe's __dmul_rn/__dadd_rn/__fma_rn/__double2float_rn on random and
+// adversarial operands.  Usage: softfp64_check_gpu <count> <seed>; prints mismatches.
 #include <cstdio>
 #include <cstdlib>
 
@@ -56,15 +57,56 @@ __global__ void check(long long count, unsigned long long seed, unsigned long lo
   if (bf) atomicAdd(&bad[2], bf);
 }
 
+// the same-binade Laplacian against the FP64 sequence it replaces, on the
+// device: one exponent field per operand set (random significands, tops of the
+// binade, few-bit significands for ties), both signs, all three stencil forms
+__global__ void check_lap(long long count, unsigned long long seed, unsigned long long *bad) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  unsigned long long bl = 0, taken = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += stride) {
+    const uint64_t r = mix(seed + 8 * i);
+    const uint64_t ef = 1 + (r >> 11) % 2043;
+    const uint64_t sg = (r >> 63) << 63;
+    double v[5];
+    for (int k = 0; k < 5; ++k) {
+      const uint64_t q = mix(seed + 8 * i + 1 + k);
+      uint64_t f;
+      switch ((r >> (2 * k)) & 3) {
+        case 0: f = q & 0x000fffffffffffffull; break;
+        case 1: f = 0x000fffffffffffffull - (q & 0xff); break;
+        case 2: f = (q & 0xf) << ((q >> 8) % 49); break;
+        default: f = (q & 0x000fffffffffffffull) | 0x000ffffff0000000ull; break;
+      }
+      v[k] = double_of(sg | (ef << 52) | f);
+    }
+    const int jcase = (int)((r >> 30) % 3);
+    const double n = v[0], s = v[1], w = jcase == 1 ? v[3] : v[2], e = jcase == 2 ? v[2] : v[3], c = v[4];
+    double want = __dadd_rn(n, s);
+    want = jcase == 0 ? __dadd_rn(__dadd_rn(want, w), e) : __fma_rn(2.0, jcase == 1 ? e : w, want);
+    want = __fma_rn(-4.0, c, want);
+    double got = 0.0;
+    if (lap_same_binade(n, s, w, e, c, jcase, &got)) {
+      ++taken;
+      if (bits_of(got) != bits_of(want)) ++bl;
+    } else if ((bits_of(want) & 0x7ff0000000000000ull) != 0) {
+      ++bl;  // a normal result must take the integer path
+    }
+  }
+  if (bl) atomicAdd(&bad[3], bl);
+  atomicAdd(&bad[4], taken);
+}
+
 int main(int argc, char **argv) {
   const long long count = argc > 1 ? atoll(argv[1]) : (1ll << 28);
   const unsigned long long seed = argc > 2 ? strtoull(argv[2], nullptr, 10) : 1;
-  unsigned long long *bad = nullptr, h[3] = {0, 0, 0};
-  if (cudaMalloc(&bad, 3 * sizeof(unsigned long long)) != cudaSuccess) return 2;
-  cudaMemset(bad, 0, 3 * sizeof(unsigned long long));
+  unsigned long long *bad = nullptr, h[5] = {0, 0, 0, 0, 0};
+  if (cudaMalloc(&bad, 5 * sizeof(unsigned long long)) != cudaSuccess) return 2;
+  cudaMemset(bad, 0, 5 * sizeof(unsigned long long));
   check<<<152 * 8, 256>>>(count, seed, bad);
+  check_lap<<<152 * 8, 256>>>(count / 4, seed, bad);
   if (cudaMemcpy(h, bad, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) return 2;
-  printf("mismatches mul %llu add %llu to_float %llu of %lld\n", h[0], h[1], h[2], count);
+  printf("mismatches mul %llu add %llu to_float %llu of %lld; lap %llu of %lld (integer path %llu)\n", h[0], h[1],
+         h[2], count, h[3], count / 4, h[4]);
   cudaFree(bad);
-  return (h[0] || h[1] || h[2]) ? 1 : 0;
+  return (h[0] || h[1] || h[2] || h[3]) ? 1 : 0;
 }
