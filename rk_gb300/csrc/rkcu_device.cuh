@@ -131,10 +131,17 @@ struct Bruss {
   template <int kExact>
   __device__ __forceinline__ double2 eval(const double2 *__restrict__ w, int p) const {
     const int k = p / N;
-    const int j = p - k * N;
+    return eval_kj<kExact>(w, p, k, p - k * N);
+  }
+  // Same, with the pair's grid row k and column j given (loops that advance
+  // p by a fixed stride track them without a division).
+  template <int kExact>
+  __device__ __forceinline__ double2 eval_kj(const double2 *__restrict__ w, int p, int k, int j) const {
     const double2 *row = w + (p - j);
     return eval_rows<kExact>(k == 0 ? row + N : row - N, row, k == N - 1 ? row - N : row + N, j);
   }
+  // pairs per grid row (the period of the column index)
+  __device__ __forceinline__ int row_pairs() const { return N; }
 
   // Same, given the grid rows above (`up`: row k-1, or row k+1 on the first row),
   // at (`cr`: row k) and below (`dn`: row k+1, or row k-1 on the last row) of the
@@ -174,6 +181,12 @@ struct Bruss {
 //   prey  f0 = c0*y0 - d0*y0*y1,  predator f1 = d1*y0*y1 - c1*y1
 struct LvPairs {
   __device__ __forceinline__ int dep_pairs() const { return 0; }
+  // no grid: the row and column a caller tracks are unused
+  __device__ __forceinline__ int row_pairs() const { return 1 << 30; }
+  template <int kExact>
+  __device__ __forceinline__ double2 eval_kj(const double2 *__restrict__ w, int p, int, int) const {
+    return eval<kExact>(w, p);
+  }
   template <int kExact>
   __device__ __forceinline__ double2 eval(const double2 *__restrict__ w, int p) const {
     using M = Arith<kExact>;
@@ -191,6 +204,11 @@ struct LvBanded {
   const double *__restrict__ r;  // r[n_pad]
   const double *__restrict__ a;  // a[n_pad][5]
   __device__ __forceinline__ int dep_pairs() const { return 1; }
+  __device__ __forceinline__ int row_pairs() const { return 1 << 30; }
+  template <int kExact>
+  __device__ __forceinline__ double2 eval_kj(const double2 *__restrict__ w, int p, int, int) const {
+    return eval<kExact>(w, p);
+  }
 
   template <int kExact>
   __device__ __forceinline__ double comp(const double *__restrict__ y, int i) const {

@@ -49,6 +49,22 @@ __device__ __forceinline__ bool stage_sync(const PlainParams &P, int c_lo, int c
 // the Laplacian on the integer pipe, the exact mode is fastest with the
 // right-hand side's products on the FP64 pipe (the tableau products stay in
 // software) at 5 CTAs, the fused mode with all plain products in software at 6.
+// A pair index with its grid row k and column j (rows of `row` pairs),
+// advanced by a fixed stride without a division.
+struct GridCursor {
+  int p, k, j;
+  __device__ __forceinline__ GridCursor(int p0, int row) : p(p0), k(p0 / row), j(p0 - (p0 / row) * row) {}
+  __device__ __forceinline__ void advance(int step, int dk, int dj, int row) {
+    p += step;
+    k += dk;
+    j += dj;
+    if (j >= row) {
+      j -= row;
+      ++k;
+    }
+  }
+};
+
 template <class Prob, int kExact>
 constexpr int plain_min_blocks() {
   return !std::is_same<Prob, Bruss>::value ? 4 : kExact == kArithFusedSoftMul ? 6 : kExact == kArithExactSoftMul ? 5 : 4;
@@ -102,6 +118,10 @@ __global__ void __launch_bounds__(kThreads, plain_min_blocks<Prob, kExact>()) pl
   const int pend = grid_sched ? P.npairs : hi;
   const int pstep = grid_sched ? G * blockDim.x : blockDim.x;
   const int dep = prob.dep_pairs();
+  // grid row and column steps of the two pair strides the loops use
+  const int rowN = prob.row_pairs();
+  const int dk_s = pstep / rowN, dj_s = pstep - dk_s * rowN;
+  const int dk_b = static_cast<int>(blockDim.x) / rowN, dj_b = static_cast<int>(blockDim.x) - dk_b * rowN;
   auto owner = [&](int p) { return p < rr * (q + 1) ? p / (q + 1) : rr + (p - rr * (q + 1)) / max(q, 1); };
   const int c_lo = owner(max(0, lo - dep));
   const int c_hi = owner(min(P.npairs - 1, max(lo, hi - 1) + dep));
@@ -126,8 +146,8 @@ __global__ void __launch_bounds__(kThreads, plain_min_blocks<Prob, kExact>()) pl
         (P.trace_y && kstep < P.trace_cap) ? P.trace_y + static_cast<size_t>(kstep) * P.npairs : nullptr;
 
     // first stage at pair p (block-inline.h:253-272)
-    auto stage_first = [&](int p) {
-      const double2 F = prob.template eval<kRhs>(ycur, p);
+    auto stage_first = [&](int p, int k, int j) {
+      const double2 F = prob.template eval_kj<kRhs>(ycur, p, k, j);
       const double2 Y = ycur[p];
       for (int l = 1; l < s; ++l) {
         double2 wv = Y;
@@ -142,8 +162,8 @@ __global__ void __launch_bounds__(kThreads, plain_min_blocks<Prob, kExact>()) pl
       P.err[p] = make_double2(M::mul(hbh[0], F.x), M::mul(hbh[0], F.y));
     };
     // intermediate stage i at pair p (block-inline.h:276-294)
-    auto stage_mid = [&](int i, int p) {
-      const double2 F = prob.template eval<kRhs>(P.w[i], p);
+    auto stage_mid = [&](int i, int p, int k, int j) {
+      const double2 F = prob.template eval_kj<kRhs>(P.w[i], p, k, j);
       for (int l = i + 1; l < s; ++l) {
         if (!P.nzA[l * kMaxStages + i]) continue;
         const double a = hA[l * kMaxStages + i];
@@ -169,9 +189,9 @@ __global__ void __launch_bounds__(kThreads, plain_min_blocks<Prob, kExact>()) pl
     };
     // last stage at pair p (block-inline.h:298-320) and its error terms (tools.h:280-288)
     ErrMax em;
-    auto stage_last = [&](int p) {
+    auto stage_last = [&](int p, int k, int j) {
       const int i = s - 1;
-      const double2 F = prob.template eval<kRhs>(P.w[i], p);
+      const double2 F = prob.template eval_kj<kRhs>(P.w[i], p, k, j);
       double2 d = P.dy[p];
       double2 e = P.err[p];
       if (P.nzb[i]) {
@@ -248,11 +268,14 @@ __global__ void __launch_bounds__(kThreads, plain_min_blocks<Prob, kExact>()) pl
           }
           const int p_hi = min(P.npairs, (c + 1) * tp);
           if (i == 0) {
-            for (int p = c * tp + threadIdx.x; p < p_hi; p += blockDim.x) stage_first(p);
+            for (GridCursor g(c * tp + threadIdx.x, rowN); g.p < p_hi; g.advance(blockDim.x, dk_b, dj_b, rowN))
+              stage_first(g.p, g.k, g.j);
           } else if (i < s - 1) {
-            for (int p = c * tp + threadIdx.x; p < p_hi; p += blockDim.x) stage_mid(i, p);
+            for (GridCursor g(c * tp + threadIdx.x, rowN); g.p < p_hi; g.advance(blockDim.x, dk_b, dj_b, rowN))
+              stage_mid(i, g.p, g.k, g.j);
           } else {
-            for (int p = c * tp + threadIdx.x; p < p_hi; p += blockDim.x) stage_last(p);
+            for (GridCursor g(c * tp + threadIdx.x, rowN); g.p < p_hi; g.advance(blockDim.x, dk_b, dj_b, rowN))
+              stage_last(g.p, g.k, g.j);
           }
           publish_tile(done, c, base + i + 1);
         }
@@ -262,22 +285,22 @@ __global__ void __launch_bounds__(kThreads, plain_min_blocks<Prob, kExact>()) pl
       }
       if (!ok) break;
     } else {
-      for (int p = p0; p < pend; p += pstep) {
-        pf_first(p + pstep);
-        stage_first(p);
+      for (GridCursor g(p0, rowN); g.p < pend; g.advance(pstep, dk_s, dj_s, rowN)) {
+        pf_first(g.p + pstep);
+        stage_first(g.p, g.k, g.j);
       }
       if (!(ok = stage_sync(P, c_lo, c_hi, ++progress, 1))) break;
       for (int i = 1; i < s - 1; ++i) {
-        for (int p = p0; p < pend; p += pstep) {
-          pf_mid(i, p + pstep);
-          stage_mid(i, p);
+        for (GridCursor g(p0, rowN); g.p < pend; g.advance(pstep, dk_s, dj_s, rowN)) {
+          pf_mid(i, g.p + pstep);
+          stage_mid(i, g.p, g.k, g.j);
         }
         if (!(ok = stage_sync(P, c_lo, c_hi, ++progress, 2))) break;
       }
       if (!ok) break;
-      for (int p = p0; p < pend; p += pstep) {
-        pf_last(p + pstep);
-        stage_last(p);
+      for (GridCursor g(p0, rowN); g.p < pend; g.advance(pstep, dk_s, dj_s, rowN)) {
+        pf_last(g.p + pstep);
+        stage_last(g.p, g.k, g.j);
       }
     }
     double emax = em.best;
