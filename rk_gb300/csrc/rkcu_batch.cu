@@ -40,19 +40,40 @@ __device__ __forceinline__ double2 batch_rhs(const InstDesc &d, const double2 *w
 template <int kT>
 __device__ void rebuild_chunks(const BatchParams &P) {
   __shared__ int s_cnt;
-  if (threadIdx.x == 0) s_cnt = 0;
+  __shared__ unsigned long long s_pairs;
+  if (threadIdx.x == 0) {
+    s_cnt = 0;
+    s_pairs = 0ull;
+  }
   __syncthreads();
   const int nslots = *(volatile int *)P.nslots;
   for (int slot = threadIdx.x; slot < nslots; slot += kT) {
     const InstDesc &d = P.desc[slot];
+    if (d.active && !d.done) atomicAdd(&s_pairs, static_cast<unsigned long long>(d.npairs));
+  }
+  __syncthreads();
+  // The tuned chunk length, shortened (a multiple of 128 pairs, at least 128)
+  // when the active pairs would give fewer than two chunks per CTA, so that a
+  // few large instances still occupy the whole grid.
+  int len = P.chunk_pairs;
+  if (P.nblocks > 0) {
+    const unsigned long long want = 2ull * static_cast<unsigned long long>(P.nblocks);
+    if (s_pairs < want * static_cast<unsigned long long>(len)) {
+      const unsigned long long l = ((s_pairs + want - 1) / want + 127) / 128 * 128;
+      len = static_cast<int>(l < 128ull ? 128ull : l);
+    }
+  }
+  for (int slot = threadIdx.x; slot < nslots; slot += kT) {
+    const InstDesc &d = P.desc[slot];
     if (!d.active || d.done) continue;
-    const int k = (d.npairs + P.chunk_pairs - 1) / P.chunk_pairs;
+    const int k = (d.npairs + len - 1) / len;
     const int base = atomicAdd(&s_cnt, k);
-    for (int j = 0; j < k; ++j) P.chunks[base + j] = make_int2(slot, j * P.chunk_pairs);
+    for (int j = 0; j < k; ++j) P.chunks[base + j] = make_int2(slot, j * len);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     *P.nchunks = s_cnt;
+    *P.chunk_len = len;
     __threadfence();
   }
 }
@@ -62,18 +83,19 @@ __global__ void __launch_bounds__(kT) batch_rebuild_kernel(const __grid_constant
   rebuild_chunks<kT>(P);
 }
 
-// resident threads per SM by mode (as for the plain kernel; measured on the
-// batched sample): 1536 fused, 1280 exact, else 1024
+// 1024 resident threads per SM (64 registers) for every block size: fewer
+// registers spill, and a single large instance then ran 2.7x slower than the
+// plain form at 256 or 128 threads per block (1.3x at 64 registers)
 template <int kExact>
 constexpr int batch_threads_per_sm() {
-  return kExact == kArithFusedSoftMul ? 1536 : kExact == kArithExactSoftMul ? 1280 : 1024;
+  return 1024;
 }
 
 template <int kExact, int kT>
 __global__ void __launch_bounds__(kT, batch_threads_per_sm<kExact>() / kT) batch_kernel(const __grid_constant__ BatchParams P) {
   using M = Arith<kExact>;
   __shared__ double s_wmax[kT / 32];
-  __shared__ int s_nch, s_rebuild;
+  __shared__ int s_nch, s_clen, s_rebuild;
   DevState *st = P.st;
   const int s = P.s;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -82,9 +104,12 @@ __global__ void __launch_bounds__(kT, batch_threads_per_sm<kExact>() / kT) batch
   bool ok = true;
 
   for (int it = 0; it < P.budget; ++it) {
-    if (threadIdx.x == 0) s_nch = *(volatile int *)P.nchunks;
+    if (threadIdx.x == 0) {
+      s_nch = *(volatile int *)P.nchunks;
+      s_clen = *(volatile int *)P.chunk_len;
+    }
     __syncthreads();
-    const int nch = s_nch;
+    const int nch = s_nch, clen = s_clen;
     if (nch == 0) break;
 
     for (int i = 0; i < s && ok; ++i) {
@@ -99,7 +124,7 @@ __global__ void __launch_bounds__(kT, batch_threads_per_sm<kExact>() / kT) batch
         double2 *__restrict__ ynew = vec + (d.cur ? 0 : np);
         double2 *__restrict__ dy = vec + static_cast<size_t>(s + 1) * np;
         double2 *__restrict__ er = vec + static_cast<size_t>(s + 2) * np;
-        const int pend = min(ch.y + P.chunk_pairs, d.npairs);
+        const int pend = min(ch.y + clen, d.npairs);
         ErrMax em;
         if (i == 0) {
           for (int p = ch.y + threadIdx.x; p < pend; p += kT) {

@@ -38,7 +38,8 @@ struct BatchParams {
   int *nslots;         // slots [0, *nslots) may be active (device, so a captured graph stays valid)
   int2 *chunks;        // (slot, first pair) of every chunk of every active instance
   int *nchunks;
-  int chunk_pairs;     // pairs per chunk
+  int chunk_pairs;     // pairs per chunk (the tuned length)
+  int *chunk_len;      // pairs per chunk of the current list (device; at most chunk_pairs)
   int *rebuild;        // set when an instance finished during a sweep
   int *done_list;      // slots that finished, in order
   int *done_count;

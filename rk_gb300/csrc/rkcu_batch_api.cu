@@ -49,7 +49,7 @@ struct rkcu_batch {
   InstCoef *d_coef = nullptr;
   int2 *d_chunks = nullptr;
   size_t chunk_cap = 0;
-  int *d_ints = nullptr;  // [0] nslots, [1] nchunks, [2] rebuild, [3] done_count
+  int *d_ints = nullptr;  // [0] nslots, [1] nchunks, [2] rebuild, [3] done_count, [4] chunk length
   int *d_done = nullptr;
   DevState *d_st = nullptr;
   char *arena = nullptr;
@@ -135,6 +135,7 @@ BatchParams make_params(rkcu_batch *b, int budget) {
   p.nchunks = b->d_ints + 1;
   p.rebuild = b->d_ints + 2;
   p.done_count = b->d_ints + 3;
+  p.chunk_len = b->d_ints + 4;
   p.done_list = b->d_done;
   p.chunks = b->d_chunks;
   p.chunk_pairs = b->chunk_pairs;
@@ -159,6 +160,7 @@ int launch(rkcu_batch *b, int budget) {
     if (!b->graph_exec || b->graph_budget != budget) {
       drop_graph(b);
       BatchParams p = make_params(b, budget);
+      p.nblocks = rkcu::batch_grid(exact, b->threads, b->blocks_per_sm, b->num_sms);
       cudaGraph_t g = nullptr;
       BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
       cudaError_t e1 = rkcu::launch_batch_rebuild(p, b->stream);
@@ -185,6 +187,7 @@ int launch(rkcu_batch *b, int budget) {
     BCK(cudaGraphLaunch(b->graph_exec, b->stream));
   } else {
     BatchParams p = make_params(b, budget);
+    p.nblocks = rkcu::batch_grid(exact, b->threads, b->blocks_per_sm, b->num_sms);
     BCK(rkcu::launch_batch_rebuild(p, b->stream));
     int grid = 0;
     BCK(rkcu::launch_batch(p, exact, b->threads, b->blocks_per_sm, b->num_sms, b->stream, &grid));
@@ -289,8 +292,8 @@ int rkcu_batch_create(rkcu_batch **out, long long arena_bytes, int max_instances
   b->chunk_cap = b->arena_bytes / (sizeof(double2) * 128) + (size_t)max_instances + 1;
   if ((e = cudaMalloc(&b->d_chunks, sizeof(int2) * b->chunk_cap)) != cudaSuccess)
     return bail(fail(b, e, "chunks"));
-  if ((e = cudaMalloc(&b->d_ints, 4 * sizeof(int))) != cudaSuccess) return bail(fail(b, e, "ints"));
-  if ((e = cudaMemset(b->d_ints, 0, 4 * sizeof(int))) != cudaSuccess) return bail(fail(b, e, "ints"));
+  if ((e = cudaMalloc(&b->d_ints, 5 * sizeof(int))) != cudaSuccess) return bail(fail(b, e, "ints"));
+  if ((e = cudaMemset(b->d_ints, 0, 5 * sizeof(int))) != cudaSuccess) return bail(fail(b, e, "ints"));
   if ((e = cudaMalloc(&b->d_done, sizeof(int) * max_instances)) != cudaSuccess)
     return bail(fail(b, e, "done list"));
   if ((e = cudaMalloc(&b->d_st, sizeof(DevState))) != cudaSuccess) return bail(fail(b, e, "state"));
