@@ -367,6 +367,8 @@ def run_ours(args):
         "clocks": clk,
         "device_bytes": dev_bytes,
     }
+    if args.precision == "mixed":
+        line["error_vs_fp64"] = mixed_error_vs_fp64(rk, prob, y0, args.method)
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         v, k, dt = cpu_baseline_port(threads)
@@ -377,6 +379,24 @@ def run_ours(args):
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+MIXED_CHECK_TE = 0.004
+
+
+def mixed_error_vs_fp64(rk, prob, y0, method):
+    """The mixed form's error, stated with its result: relative max-norm difference at
+    t = MIXED_CHECK_TE between the mixed form and the exact FP64 form (which is
+    bit-identical to the reference) from the same initial values at tol 1e-6.  A short
+    interval keeps the FP64 solve to a few seconds at N=4000; the full-interval errors
+    at N up to 2000 are in the mixed-precision tests."""
+    with rk.Solver(prob, method=method, precision="exact") as s:
+        ref, rst = s.solve(T0, MIXED_CHECK_TE, y0, TOL)
+    with rk.Solver(prob, method=method, precision="mixed") as s:
+        y, st = s.solve(T0, MIXED_CHECK_TE, y0, TOL)
+    err = float(np.max(np.abs(y - ref)) / np.max(np.abs(ref)))
+    return {"t_end": MIXED_CHECK_TE, "rel_max_norm": err, "tol": TOL, "within_tol": err <= TOL,
+            "steps_mixed": st["steps_acc"] + st["steps_rej"], "steps_fp64": rst["steps_acc"] + rst["steps_rej"]}
 
 
 def run_batched(args):
