@@ -104,6 +104,33 @@ def test_tuning_and_graph_replay_change_nothing():
         np.testing.assert_array_equal(a[k][0], b[k][0])
 
 
+def test_large_instance_same_under_every_shape():
+    """One instance whose pairs (N=256: 65536) are far fewer than two tuned chunks per CTA,
+    so the chunk list is built with shortened chunks; every block size and tuned chunk
+    length gives the same result."""
+    p = rk.bruss2d_mix(256, 2e-3)
+    y0 = rk.ode_start(p)
+    with rk.Solver(p, method="DOPRI54", precision="exact") as s:
+        ref, rst = s.solve(0.0, 0.02, y0, 1e-6)
+    results = []
+    for threads, chunk in ((128, 256), (256, 1024), (256, 4096), (512, 4096)):
+        with rk.Batch(rk.footprint(p, 7) + (64 << 20), 4, precision="exact") as b:
+            b.set_tuning(threads, chunk)
+            assert b.add(p, y0, 0.0, 0.02, 1e-6, host_id=0) is not None
+            while b.run(64) > 0:
+                pass
+            b.run(1)
+            (slot,) = b.finished()
+            y, st, _ = b.take(slot)
+        results.append((y, st))
+    for y, st in results[1:]:
+        np.testing.assert_array_equal(y, results[0][0])
+        assert (st["steps_acc"], st["steps_rej"]) == (results[0][1]["steps_acc"], results[0][1]["steps_rej"])
+    # the plain form may differ only where the batch keeps a correctly rounded
+    # step-size factor that the C library rounds the other way
+    assert float(np.max(np.abs(results[0][0] - ref)) / np.max(np.abs(ref))) <= 1e-6
+
+
 def test_admission_by_hbm_footprint():
     p = rk.bruss2d_mix(64, 2e-3)
     y0 = rk.ode_start(p)
