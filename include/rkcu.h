@@ -88,7 +88,9 @@ typedef struct
   int schedule;         /* plain form, stage synchronisation: 0 = automatic (neighbour
                            flags), 1 = grid barrier after every stage, 2 = neighbour
                            progress flags, 3 = dataflow over (stage, tile) in wavefront
-                           order; mixed form: 1 = tiles with plain loads, else TMA */
+                           order; mixed form: 1 = tiles with plain loads, else TMA;
+                           low-storage form: 1 = grid barrier after every wavefront
+                           step, else neighbour progress flags */
   int flow_skew;        /* schedule 3: tiles by which stage i trails stage i-1 in the
                            wavefront; 0 = automatic (tiles are block_rows grid rows) */
 } rkcu_options;

@@ -476,6 +476,9 @@ int rkcu_advance(rkcu_solver *s, int max_steps) {
     q.st = s->st;
     q.bruss.N = N;
     q.bruss.coef = bruss_coef(&s->prob);
+    // automatic (0): neighbour flags between wavefront steps; 1: a grid barrier per step
+    q.flags = s->flags;
+    q.sync = s->opt.schedule == 1 ? 1 : 0;
     int grid = 0;
     cudaError_t e = rkcu::launch_lowstorage(q, s->opt.precision != RKCU_FP64_FMA, s->num_sms,
                                             s->stream, &grid);

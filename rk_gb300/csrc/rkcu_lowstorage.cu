@@ -6,8 +6,14 @@
 // nb + 2(s-1) steps tau; at wavefront step tau, stage i works on block
 // b = tau - 2i.  With this skew of two, everything stage i reads on blocks
 // b-1, b, b+1 was completed at an earlier tau, and no stage reads a block
-// another stage writes at the same tau, so one grid barrier per tau suffices
-// and all stages of a wavefront step run concurrently.
+// another stage writes at the same tau, so all stages of a wavefront step run
+// concurrently and one synchronisation per tau suffices: either a grid
+// barrier, or (the default) neighbour flags.  With flags every CTA works on
+// the same slice of block positions in every active block, and before tau it
+// waits only for the CTAs whose slices hold the rows its stencils read (the
+// rows next to its slice in the same block, and the edge rows of the blocks
+// before and after): each read-after-write and each ring-slot reuse is
+// between such neighbours and at least one tau apart.
 //
 // Storage: y (two full vectors, ping-pong as in the plain form) plus ring
 // buffers: w_l keeps the blocks from tau-2l-1 to tau (2l+2 slots), dy and err
@@ -21,6 +27,42 @@
 namespace rkcu {
 
 constexpr int kLsThreads = 256;
+
+// Wait until every CTA in the ranges [lo[r], hi[r]] (other than this one) has
+// published at least `target` -- one polling thread per CTA, each bounded by
+// the time limit -- then a CTA barrier.  False on a time-out or an error set
+// elsewhere.
+__device__ bool wait_ranges(const unsigned int *flags, const int *lo, const int *hi, int nr,
+                            unsigned int target, DevState *st, unsigned long long timeout_ns,
+                            int site) {
+  int bad = 0;
+  int base = 0;
+  for (int r = 0; r < nr; ++r) {
+    const int cnt = hi[r] - lo[r] + 1;
+    for (int q = static_cast<int>(threadIdx.x) - base; q < cnt && !bad; q += blockDim.x) {
+      if (q < 0) continue;
+      const int c = lo[r] + q;
+      if (c == static_cast<int>(blockIdx.x)) continue;
+      const unsigned long long t0 = globaltimer_ns();
+      unsigned int ns = 32;
+      while (ld_acquire(&flags[c]) < target) {
+        if (*(volatile int *)&st->error) {
+          bad = 1;
+          break;
+        }
+        if (globaltimer_ns() - t0 > timeout_ns) {
+          if (atomicCAS(&st->error, 0, 1) == 0) st->error_site = site;
+          bad = 1;
+          break;
+        }
+        __nanosleep(ns);
+        if (ns < 256) ns <<= 1;
+      }
+    }
+    base += cnt > 0 ? cnt : 0;
+  }
+  return !__syncthreads_or(bad);
+}
 
 template <int kExact>
 __global__ void __launch_bounds__(kLsThreads, 4) ls_kernel(const __grid_constant__ LsParams P) {
@@ -42,6 +84,10 @@ __global__ void __launch_bounds__(kLsThreads, 4) ls_kernel(const __grid_constant
   __shared__ const double2 *s_rd[kMaxStages][3];
   __shared__ double2 *s_wr[kMaxStages][kMaxStages];
   __shared__ double2 *s_dyb[kMaxStages], *s_erb[kMaxStages];
+  // neighbour flags: this CTA's slice of each active item (first pair in the
+  // block, start in the CTA's own list), and the CTAs it depends on
+  __shared__ int s_mlo[kMaxStages], s_mstart[kMaxStages + 1];
+  __shared__ int s_rlo[3], s_rhi[3], s_nr;
 
   DevState *st = P.st;
   const int s = P.s, N = P.N, R = P.R, nb = P.nb;
@@ -62,7 +108,37 @@ __global__ void __launch_bounds__(kLsThreads, 4) ls_kernel(const __grid_constant
     s_pend_err = st->pend_err;
     s_pend_h = st->pend_h;
   }
+  const bool flags = P.sync == 0;
+  const int G = gridDim.x;
+  if (flags && threadIdx.x == 0) {
+    // Slices: CTA c takes the block positions [c R N / G, (c+1) R N / G) of
+    // every block (truncated in a shorter last block), so a ring slot's
+    // position belongs to the same CTA whichever block it holds.  The stencils
+    // of a slice read the rows next to it in its block, the previous block's
+    // last row if it starts the block, the next block's first row if it ends
+    // it; the CTAs reading the slice are the same ones.
+    const int c = blockIdx.x;
+    const int npf = R * N;
+    auto owner = [&](long long q) { return static_cast<int>(((q + 1) * G - 1) / npf); };
+    int nr = 0;
+    const long long a = static_cast<long long>(c) * npf / G, e = static_cast<long long>(c + 1) * npf / G;
+    if (a < e) {
+      const int k0 = static_cast<int>(a / N), k1 = static_cast<int>((e - 1) / N);
+      s_rlo[nr] = owner(k0 > 0 ? static_cast<long long>(k0 - 1) * N : 0);
+      s_rhi[nr++] = owner(k1 + 2 < R ? static_cast<long long>(k1 + 2) * N - 1 : npf - 1);
+      if (k0 == 0 && nb > 1) {
+        s_rlo[nr] = owner(static_cast<long long>(R - 1) * N);
+        s_rhi[nr++] = G - 1;
+      }
+      if (k1 == R - 1 && nb > 1) {
+        s_rlo[nr] = 0;
+        s_rhi[nr++] = owner(N - 1);
+      }
+    }
+    s_nr = nr;
+  }
   __syncthreads();
+  unsigned int progress = 0;  // wavefront steps this CTA has completed in this launch
 
   bool ok = true;
   for (int it = 0; it < P.budget; ++it) {
@@ -95,6 +171,17 @@ __global__ void __launch_bounds__(kLsThreads, 4) ls_kernel(const __grid_constant
         }
         s_start[cnt] = off;
         s_nact = cnt;
+        int mine = 0;
+        const long long npf = static_cast<long long>(R) * N;
+        for (int a = 0; a < cnt; ++a) {
+          const int np = s_start[a + 1] - s_start[a];
+          const int lo = min(np, static_cast<int>(static_cast<long long>(blockIdx.x) * npf / G));
+          const int hi = min(np, static_cast<int>(static_cast<long long>(blockIdx.x + 1) * npf / G));
+          s_mlo[a] = lo;
+          s_mstart[a] = mine;
+          mine += hi - lo;
+        }
+        s_mstart[cnt] = mine;
       }
       __syncthreads();
       if (threadIdx.x < s_nact) {
@@ -115,13 +202,22 @@ __global__ void __launch_bounds__(kLsThreads, 4) ls_kernel(const __grid_constant
       }
       __syncthreads();
       const int nact = s_nact;
-      const int total = s_start[nact];
-      for (int u = gtid; u < total; u += gstride) {
+      // neighbour flags: the CTAs this slice reads have completed tau - 1
+      // (tau 0 follows the step's grid barrier)
+      if (flags && tau > 0 &&
+          !(ok = wait_ranges(P.flags, s_rlo, s_rhi, s_nr, progress, st, P.timeout_ns, 32)))
+        break;
+      // flags: this CTA's slices (its own list, block stride); grid barrier:
+      // all items' pairs over the grid
+      const int total = flags ? s_mstart[nact] : s_start[nact];
+      for (int u = flags ? static_cast<int>(threadIdx.x) : gtid; u < total;
+           u += flags ? static_cast<int>(blockDim.x) : gstride) {
         int a = 0;
-        while (a + 1 < nact && u >= s_start[a + 1]) ++a;
+        const int *starts = flags ? s_mstart : s_start;
+        while (a + 1 < nact && u >= starts[a + 1]) ++a;
         const int i = s_stage[a];
         const int b = s_blk[a];
-        const int q = u - s_start[a];
+        const int q = flags ? s_mlo[a] + (u - s_mstart[a]) : u - s_start[a];
         const int r = static_cast<int>((static_cast<unsigned long long>(q) * P.inv_n) >> 40);
         const int j = q - r * N;
         const int k = b * R + r;  // grid row
@@ -194,7 +290,10 @@ __global__ void __launch_bounds__(kLsThreads, 4) ls_kernel(const __grid_constant
           }
         }
       }
-      ok = grid_barrier(st, P.nblocks, P.timeout_ns, 30);
+      if (flags)
+        publish_progress(P.flags, ++progress);
+      else
+        ok = grid_barrier(st, P.nblocks, P.timeout_ns, 30);
     }
     if (!ok) break;
 
@@ -277,6 +376,10 @@ static cudaError_t launch_t(const LsParams &p, int num_sms, cudaStream_t stream,
   int grid = occ * num_sms;
   LsParams q = p;
   q.nblocks = grid + (p.extra_arrivals > 0 ? p.extra_arrivals : 0);
+  if (q.sync == 0) {
+    e = cudaMemsetAsync(q.flags, 0, sizeof(unsigned int) * grid, stream);
+    if (e != cudaSuccess) return e;
+  }
   void *args[] = {&q};
   *grid_out = grid;
   return cudaLaunchCooperativeKernel((const void *)ls_kernel<kExact>, dim3(grid), dim3(kLsThreads),

@@ -20,6 +20,8 @@ struct LsParams {
   double2 *dyring, *errring;     // 2s-1 block slots each
   DevState *st;
   Bruss bruss;
+  unsigned int *flags;           // per-CTA progress (zeroed by each launch), gridDim.x words
+  int sync;                      // 0: neighbour flags between wavefront steps, 1: grid barrier
 };
 
 cudaError_t launch_lowstorage(const LsParams &p, bool exact, int num_sms, cudaStream_t stream,

@@ -59,6 +59,29 @@ def test_lowstorage_fma_equals_plain_fma(method):
     np.testing.assert_array_equal(a, b)
 
 
+@pytest.mark.parametrize("N,rows,method", [(2000, 0, "DOPRI54"), (300, 64, "DOPRI54"), (7, 2, "DOPRI54"),
+                                           (2, 1, "DOPRI54"), (150, 32, "DOPRI87")])
+def test_lowstorage_neighbour_flags_equal_grid_barrier(N, rows, method):
+    """The neighbour-flag synchronisation between wavefront steps (the default) and a
+    grid barrier per step give the same bits: blocks that do not divide the grid
+    (N=2000 with R=64 leaves a 16-row last block), CTAs without work (tiny grids), and
+    the 13-stage tableau."""
+    prob = rk.bruss2d_mix(N, 2e-3)
+    y0 = rk.ode_start(prob)
+    te = 0.002 if N >= 1000 else 0.05
+    out = []
+    for schedule in (0, 1):
+        with rk.Solver(prob, method=method, variant=rk.VARIANT_LOWSTORAGE, block_rows=rows,
+                       schedule=schedule) as s:
+            out.append(s.solve(0.0, te, y0, 1e-6))
+    (a, sa), (b, sb) = out
+    assert (sa["steps_acc"], sa["steps_rej"]) == (sb["steps_acc"], sb["steps_rej"])
+    np.testing.assert_array_equal(a, b)
+    with rk.Solver(prob, method=method, schedule=0) as s:
+        c, sc = s.solve(0.0, te, y0, 1e-6)
+    np.testing.assert_array_equal(a, c)
+
+
 def test_lowstorage_rejects_other_problems():
     with pytest.raises(rk.RkcuError) as ei:
         rk.Solver(rk.lv_pairs(10), variant=rk.VARIANT_LOWSTORAGE)
