@@ -76,7 +76,9 @@ def fp64_ops_per_comp(method, precision):
     point), so a right-hand side keeps 2.5 sums per component; in the exact
     mode its 3 products per component run on the FP64 pipe (with max/compare
     work 6.3 per right-hand side) while the tableau products run in software
-    binary64 on the integer pipe; the fused mode keeps 3.5 per right-hand side.
+    binary64 on the integer pipe; the fused mode keeps 3.3 per right-hand side
+    and computes the first stage's two plain products in software (ncu: 53.7
+    FP64-pipe instructions per DOPRI5(4) component-step, 73.4 exact).
     The mixed form evaluates F0 in double-float arithmetic (FP32 pairs, the
     Laplacian in integer fixed point) and keeps three FP64 sums per
     component-step: y + (h sum b F0) as two sums, and y1 + dY."""
@@ -94,7 +96,7 @@ def fp64_ops_per_comp(method, precision):
             return 5.5 * s + 2 * nz_a + (2 * nz_b - 1) + (2 * nz_bh - 1) + 1.5, ops
         return 6.3 * s + nz_a + (nz_b - 1) + (nz_bh - 1) + 1.5, ops
     ops = 7.5 * s + nz_a + nz_b + nz_bh + 1.5
-    return 3.5 * s + nz_a + nz_b + nz_bh + 1.5, ops
+    return 3.3 * s + nz_a + (nz_b - 1) + (nz_bh - 1) + 1.5, ops
 
 
 def _peaks():
