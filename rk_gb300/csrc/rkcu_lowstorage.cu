@@ -23,6 +23,7 @@
 // order as in the plain form, so results are bit-identical to it.
 #include "rkcu.h"
 #include "rkcu_lowstorage.cuh"
+#include "rkcu_plain.cuh"  // kMaxPlainGrid: the progress words a solver allocates
 
 namespace rkcu {
 
@@ -376,6 +377,7 @@ static cudaError_t launch_t(const LsParams &p, int num_sms, cudaStream_t stream,
   int grid = occ * num_sms;
   LsParams q = p;
   q.nblocks = grid + (p.extra_arrivals > 0 ? p.extra_arrivals : 0);
+  if (q.sync == 0 && (q.flags == nullptr || grid > kMaxPlainGrid)) q.sync = 1;  // more CTAs than flag words
   if (q.sync == 0) {
     e = cudaMemsetAsync(q.flags, 0, sizeof(unsigned int) * grid, stream);
     if (e != cudaSuccess) return e;
