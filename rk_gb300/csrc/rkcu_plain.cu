@@ -17,6 +17,13 @@
 // last stage before the error max is read.  The error max is reduced by warp
 // shuffles, shared memory and one 64-bit atomicMax per CTA on the bit pattern
 // (the values are >= 0).
+//
+// Arithmetic per mode (all modes give the hardware's bits): the exact mode
+// runs the tableau products in software binary64 and the right-hand side's
+// products on the FP64 pipe, the fused mode its remaining plain products in
+// software; in every mode the right-hand side's Laplacian sums run in exact
+// integer arithmetic where the operands share a binade.  Resident CTAs per SM
+// are set per mode (plain_min_blocks).
 #include <type_traits>
 
 #include "rkcu_plain.cuh"
