@@ -10,7 +10,9 @@
 //   error    per-chunk block reduction, 64-bit atomicMax into the instance
 //   control  one thread per instance: accept/reject, step size (correctly
 //            rounded pow), t, counters, next h*A (include/tools.h:191-278)
-//   compact  when an instance finished, CTA 0 rebuilds the chunk list
+//   compact  when an instance finished, CTA 0 rebuilds the chunk list; the
+//            chunk length is the tuned one, shortened when the active pairs
+//            would give fewer than two chunks per CTA (a few large instances)
 // Instances are independent, so no problem ever waits for another one's data;
 // the only synchronisation is the grid barrier between stages.
 #include "rkcu.h"
