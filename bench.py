@@ -212,36 +212,101 @@ def cpu_baseline_port(threads, target_s=12.0, max_steps=400):
     return done / dt, done, dt
 
 
+REF_VARIANT = "pthreads/PipeD4ls"
+
+
+def reference_run(steps, threads, grid_n=GRID_N):
+    """Run the reference's own pthreads PipeD4ls solver (its fastest variant),
+    compiled from its sources with its own flags and the workload's defines,
+    for `steps` attempted steps (the STEP_LIMIT define).  Returns (steps done,
+    the solver's own "Kernel time" in s), or None without reference sources or
+    a C compiler."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import stage_reference
+    defines = dict(BRUSS_GRID_SIZE=grid_n, BRUSS_ALPHA="2E-3", METHOD="DOPRI54", TOL="1E-6",
+                   T_END="0.5", STEP_LIMIT=int(steps))
+    try:
+        exe = stage_reference.build_solver(REF_VARIANT, defines,
+                                           name=f"pthreads_bruss2d-mix_PipeD4ls_n{grid_n}_l{steps}")
+    except Exception:
+        return None
+    if not exe:
+        return None
+    out = subprocess.run([exe], env=dict(os.environ, NUM_THREADS=str(threads)), capture_output=True,
+                         text=True, check=True).stdout
+    import re
+    m = re.search(r"Number of steps: (\d+)", out)
+    k = re.search(r"Kernel time: ([0-9.eE+-]+) s", out)
+    return int(m.group(1)), float(k.group(1))
+
+
+def cpu_baseline(threads, target_s=10.0, max_steps=400, min_steps=2):
+    """The CPU baseline on the full-size problem: the reference's own PipeD4ls
+    binary when its sources are here (kind "reference"), else the oracle port in
+    the same schedule (kind "port").  As many steps as fit in about target_s.
+    Returns (steps/s, steps, seconds, kind, description)."""
+    probe = reference_run(5, threads)
+    if probe is not None:
+        per = probe[1] / max(1, probe[0])
+        steps = int(max(min_steps, min(max_steps, target_s / max(per, 1e-6))))
+        done, kt = reference_run(steps, threads)
+        return done / kt, done, kt, "reference", (
+            f"the reference's {REF_VARIANT} solver compiled from its sources (-O3 -g, its "
+            f"flags), first {done} steps of the N={GRID_N} solve (STEP_LIMIT={steps}), "
+            f"{threads} threads, its own Kernel time")
+    v, done, dt = cpu_baseline_port(threads, target_s, max_steps)
+    return v, done, dt, "port", (f"first {done} steps of the same N={GRID_N} solve ({dt:.1f} s), "
+                                 f"oracle port, {PORT_SCHEDULE}, {threads} pthreads")
+
+
+def workload_config(grid_n, method, ws):
+    """The `config` both arms print: the workload, not the implementation."""
+    n = 2 * grid_n * grid_n
+    return {"workload": f"bruss2d-mix N={grid_n} n={n} {method} tol=1e-6 t=[0,0.5]",
+            "grid_n": grid_n, "alpha": ALPHA, "method": method, "tol": TOL, "t_end": TE,
+            "parallelism": f"replicas{ws}",
+            "l2": f"working set {(10 if method == 'DOPRI54' else 16) * 8 * n / 1e6:.0f} MB "
+                  f"> {L2_BYTES / 1e6:.0f} MB L2, no flush"}
+
+
 def run_reference(args):
     ws, rank, local = _dist()
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
-    # each "step" of this arm is one RK step on the full problem; the sample is
-    # bounded so the whole run ends within a few minutes
-    sys.path.insert(0, os.path.join(REPO, "oracle"))
-    import rk_oracle
-    y0 = rk_oracle.bruss_start(GRID_N)
-    t = time.perf_counter()
-    port_solve(rk_oracle, y0, TOL, max(1, args.warmup), threads)
-    warm = time.perf_counter() - t
-    per = warm / max(1, args.warmup)
-    k = max(2, min(args.steps, int(150.0 / max(per, 1e-6))))
-    t = time.perf_counter()
-    _, st = port_solve(rk_oracle, y0, TOL, k, threads)
-    dt = time.perf_counter() - t
-    k = st["steps_acc"] + st["steps_rej"]
+    # warm-up run, then the timed sample: each "step" is one RK step on the full
+    # problem, the sample bounded so that the whole run ends within a few minutes
+    probe = reference_run(max(1, args.warmup), threads)
+    if probe is not None:
+        per = probe[1] / max(1, probe[0])
+        k = max(2, min(args.steps, int(90.0 / max(per, 1e-6))))
+        k, dt = reference_run(k, threads)
+        kind, sample = "reference", (f"the reference's {REF_VARIANT} solver compiled from its "
+                                     f"sources, first {k} steps of the N={GRID_N} solve, "
+                                     f"{threads} threads, its own Kernel time")
+    else:
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import rk_oracle
+        y0 = rk_oracle.bruss_start(GRID_N)
+        t = time.perf_counter()
+        port_solve(rk_oracle, y0, TOL, max(1, args.warmup), threads)
+        per = (time.perf_counter() - t) / max(1, args.warmup)
+        k = max(2, min(args.steps, int(90.0 / max(per, 1e-6))))
+        t = time.perf_counter()
+        _, st = port_solve(rk_oracle, y0, TOL, k, threads)
+        dt = time.perf_counter() - t
+        k = st["steps_acc"] + st["steps_rej"]
+        kind, sample = "port", (f"first {k} steps of the N={GRID_N} solve, oracle port "
+                                f"({PORT_SCHEDULE}), {threads} pthreads")
     v = k / dt
     line = {
-        "impl": "reference", "metric": "BRUSS2D-MIX N=2000 DOPRI54 steps/s", "value": v,
+        "impl": "reference", "metric": f"BRUSS2D-MIX N={GRID_N} DOPRI54 steps/s", "value": v,
         "unit": "steps/s", "n_gpus": args.gpus, "steps": k, "warmup": args.warmup,
         "ms_per_step": 1e3 * dt / k, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (ode_start initial values)",
-        "config": {"workload": "bruss2d-mix N=2000 n=8e6 DOPRI54 tol=1e-6 t=[0,0.5]",
-                   "grid_n": GRID_N, "alpha": ALPHA, "method": "DOPRI54"},
-        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
-                         "sample": f"first {k} steps of the N=2000 solve, {PORT_SCHEDULE}, "
-                                   f"{threads} pthreads"},
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (ode_start initial values of BRUSS2D-MIX)",
+        "config": workload_config(GRID_N, "DOPRI54", ws),
+        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads, "kind": kind,
+                         "sample": sample},
         "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -343,10 +408,9 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision != "mixed" else "f32 stages / f64 state",
         "data": "synthetic (ode_start initial values of BRUSS2D-MIX)",
-        "config": {"workload": f"bruss2d-mix N={args.grid} n={n} {args.method} tol=1e-6 t=[0,0.5]",
-                   "grid_n": args.grid, "alpha": ALPHA, "method": args.method,
-                   "precision": args.precision, "variant": args.variant, "parallelism": f"replicas{ws}",
-                   "l2": f"per-step working set {dev_bytes / 1e6:.0f} MB > {L2_BYTES / 1e6:.0f} MB L2, no flush"},
+        "config": workload_config(args.grid, args.method, ws),
+        "implementation": {"precision": args.precision, "variant": args.variant,
+                           "device_working_set_mb": round(dev_bytes / 1e6)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "traffic_bytes_per_component_step": tr[0] if tr else None,
@@ -371,16 +435,220 @@ def run_ours(args):
     }
     if args.precision == "mixed":
         line["error_vs_fp64"] = mixed_error_vs_fp64(rk, prob, y0, args.method)
-    if not args.no_cpu_baseline:
+    if not args.no_cpu_baseline and args.grid == GRID_N and args.method == "DOPRI54":
         threads = os.cpu_count() or 1
-        v, k, dt = cpu_baseline_port(threads)
-        line["cpu_baseline"] = {"value": v, "unit": "steps/s", "cores": threads, "kind": "port",
-                                "sample": f"first {k} steps of the same N=2000 solve ({dt:.1f} s), "
-                                          f"{PORT_SCHEDULE}, {threads} pthreads"}
+        v, k, dt, kind, sample = cpu_baseline(threads)
+        line["cpu_baseline"] = {"value": v, "unit": "steps/s", "cores": threads, "kind": kind,
+                                "sample": sample}
+    if ws == 1 and not args.no_forms and args.grid == GRID_N and args.method == "DOPRI54":
+        # the metric's second half: batched solves/s, served p50/p99 against the
+        # plain form, and the mixed-precision configuration, each timed on its own
+        line["mixed"] = form_mixed(rk, local, peak, peak_kind)
+        line["batched"] = form_batched(rk, args.batched_sample, not args.no_cpu_baseline)
+        cap = line["batched"]["component_steps_per_s"]
+        line["served"] = [form_served(rk, args.served_requests, load, cap) for load in (0.5, 0.9)]
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def form_mixed(rk, device, peak, peak_kind):
+    """The mixed-precision configuration, whole: BRUSS2D-MIX N=4000 (n = 3.2e7),
+    DOPRI5(4), tol 1e-6, t in [0, 0.5], through the C ABI with host buffers
+    (pinned y0 in, y out).  value: attempted steps over the device time of the
+    step loop (CUDA events on the solver's stream); e2e: the same steps over
+    the host time of begin + steps + get_y.  The error is measured against the
+    exact FP64 form's final state (bit-identical to the reference wherever
+    compared) at the fixture's stored components."""
+    import torch
+    sys.path.insert(0, os.path.join(REPO, "tests", "golden"))
+    from make_n4000_fixture import sample_indices
+    base = os.path.join(REPO, "tests", "golden", "n4000", "bruss_n4000_dopri54_tol1e-6")
+    with open(base + ".json") as f:
+        rec = json.load(f)
+    ref = np.load(base + "_sample.npy")
+    idx = sample_indices(rec["grid_n"])
+    prob = rk.bruss2d_mix(rec["grid_n"], rec["alpha"])
+    n = prob.n
+    y0 = torch.from_numpy(rk.ode_start(prob)).pin_memory()
+    y = torch.empty(n, dtype=torch.float64).pin_memory()
+    stream = torch.cuda.Stream(device=device)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with rk.Solver(prob, method="DOPRI54", precision="mixed", device=device,
+                   stream=stream.cuda_stream) as s:
+        lib = rk.load()
+        torch.cuda.synchronize()
+        clocks = ClockSampler(device)
+        clocks.start()
+        t = time.perf_counter()
+        import ctypes
+        assert lib.rkcu_begin(s._h, rec["t0"], rec["t_end"], ctypes.c_void_p(y0.data_ptr()), 0,
+                              rec["tol"]) == 0
+        ev0.record(stream)
+        st = s.run(1 << 30)
+        ev1.record(stream)
+        assert lib.rkcu_get_y(s._h, ctypes.c_void_p(y.data_ptr()), 0) == 0
+        e2e_s = time.perf_counter() - t
+        ev1.synchronize()
+        clk = clocks.stop()
+        launches = s.launches
+    ms = ev0.elapsed_time(ev1)
+    steps = st["steps_acc"] + st["steps_rej"]
+    yv = y.numpy()
+    err = float(np.max(np.abs(yv[idx] - ref)) / np.max(np.abs(ref)))
+    achieved = 16.0 * n * steps / (ms * 1e-3) / 1e9
+    tr = MEASURED_TRAFFIC.get(("d", "mixed", "DOPRI54"))
+    return {
+        "metric": "mixed-precision BRUSS2D-MIX N=4000 steps/s", "value": steps / (ms * 1e-3),
+        "unit": "steps/s", "steps": steps, "accepted": st["steps_acc"], "rejected": st["steps_rej"],
+        "ms_per_step": ms / steps, "dtype": "f32 stages / f64 state", "gpu_launches": launches,
+        "config": {"workload": f"bruss2d-mix N={rec['grid_n']} n={n} DOPRI54 tol=1e-6 t=[0,0.5], "
+                               "the whole solve", "l2": "2 x 256 MB FP64 state + 7 x 128 MB FP32 "
+                               "vectors > 129 MB L2, no flush"},
+        "e2e": {"value": steps / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": 8.0 * n / steps,
+                "d2h_bytes_per_step": 8.0 * n / steps},
+        "error_vs_fp64": {"t_end": rec["t_end"], "rel_max_norm_on_sample": err,
+                          "sample": f"{idx.size} components (grid rows 0 and {rec['grid_n'] - 1}, "
+                                    "every 977th component)",
+                          "fp64_steps": rec["steps"], "tol": rec["tol"], "within_tol": err <= rec["tol"],
+                          "rel_max_norm_all_components_when_fixture_was_made":
+                              rec["mixed"]["rel_max_norm_full"]},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic_bytes_per_component_step": tr[0] if tr else None,
+                     "traffic_source": tr[1] if tr else None},
+        "clocks": clk,
+    }
+
+
+def form_batched(rk, count, cpu):
+    """Batched configuration on a seeded sample of its 4096-instance list (N
+    log-uniform [16,512], alpha U[1e-3,1e-2], tol log-uniform [1e-8,1e-4],
+    DOPRI5(4), t in [0, 0.5]): one batch, solves/s on the device (CUDA events
+    from the first sweep to the last), e2e with the admissions (host y0 copies)
+    and the result copies; the plain form and the CPU port solving the SAME
+    instances one after another (plain) and one per host thread (CPU)."""
+    import concurrent.futures as cf
+
+    import torch
+
+    from rk_gb300 import workloads
+
+    insts = workloads.batched_instances(4096, seed=2024)
+    rng = np.random.default_rng(5)
+    pick = sorted(rng.choice(len(insts), count, replace=False))
+    sample = [insts[i] for i in pick]
+    probs = [rk.bruss2d_mix(d["grid_n"], d["alpha"]) for d in sample]
+    y0s = [rk.ode_start(p) for p in probs]
+    arena = sum(rk.footprint(p, 7) for p in probs) + (64 << 20)
+    clocks = ClockSampler(0)
+    clocks.start()
+    with rk.Batch(arena, len(sample) + 1, precision="exact") as b:
+        t_e2e = time.perf_counter()
+        for k, (p, y0, d) in enumerate(zip(probs, y0s, sample)):
+            assert b.add(p, y0, d["t0"], d["te"], d["tol"], host_id=k) is not None
+        stream = torch.cuda.ExternalStream(b.stream)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        sweeps = 0
+        while b.run(256) > 0:
+            sweeps += 256
+        ev1.record(stream)
+        ev1.synchronize()
+        results = {}
+        for slot in b.finished():
+            y, st, hid = b.take(slot)
+            results[hid] = (y, st)
+        e2e_s = time.perf_counter() - t_e2e
+        info = b.info()
+        tuning = b.tuning()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    comp_steps = sum(p.n * (results[k][1]["steps_acc"] + results[k][1]["steps_rej"])
+                     for k, p in enumerate(probs))
+    host_pow = sum(results[k][1]["host_pow_steps"] for k in results)
+    # the plain form on the same instances, one after another
+    t = time.perf_counter()
+    same = 0
+    for k, (p, y0, d) in enumerate(zip(probs, y0s, sample)):
+        with rk.Solver(p, method="DOPRI54", precision="exact") as s:
+            y, st = s.solve(d["t0"], d["te"], y0, d["tol"])
+        same += int(np.array_equal(y, results[k][0]))
+    plain_s = time.perf_counter() - t
+    out = {
+        "metric": "batched BRUSS2D-MIX solves/s", "value": len(sample) / (ms * 1e-3),
+        "unit": "solves/s", "instances": len(sample), "sweeps": sweeps, "dtype": "f64",
+        "config": {"workload": f"batched: {len(sample)} of the 4096 seeded instances (seed 2024, "
+                               f"sample seed 5), {100.0 * len(sample) / 4096:.1f} % of the list",
+                   "tuning": tuning},
+        "component_steps_per_s": comp_steps / (ms * 1e-3),
+        "e2e": {"value": len(sample) / e2e_s, "unit": "solves/s",
+                "h2d_bytes_per_step": sum(8 * p.n for p in probs) / max(1, sweeps),
+                "d2h_bytes_per_step": sum(8 * p.n for p in probs) / max(1, sweeps)},
+        "plain_form": {"value": len(sample) / plain_s, "unit": "solves/s",
+                       "sample": "the same instances, one solve after another (host buffers)",
+                       "results_bit_identical_to_batch": same},
+        "host_pow_steps": host_pow, "gpu_launches": info["launches"], "clocks": clk,
+    }
+    if cpu:
+        sys.path.insert(0, os.path.join(REPO, "oracle"))
+        import rk_oracle
+        rk_oracle.load()
+        threads = os.cpu_count() or 1
+
+        def one(k):
+            d = sample[k]
+            return port_solve(rk_oracle, y0s[k], d["tol"], 0, 1, grid_n=d["grid_n"],
+                              alpha=d["alpha"], t0=d["t0"], te=d["te"])
+        t = time.perf_counter()
+        with cf.ThreadPoolExecutor(threads) as ex:
+            outs = list(ex.map(one, range(len(sample))))
+        cpu_s = time.perf_counter() - t
+        same = sum(int(np.array_equal(o[0], results[k][0])) for k, o in enumerate(outs))
+        out["cpu_baseline"] = {"value": len(sample) / cpu_s, "unit": "solves/s", "cores": threads,
+                               "kind": "port",
+                               "sample": f"the same {len(sample)} instances, one per host thread "
+                                         f"({cpu_s:.1f} s); the reference fixes N and alpha at "
+                                         "compile time, so its oracle port solves them",
+                               "results_bit_identical_to_batch": same}
+    return out
+
+
+def form_served(rk, count, load, capacity):
+    """Served configuration on the first `count` requests of the seeded
+    20,000-request Poisson stream, arrivals rescaled so that the offered work
+    is `load` times the batched capacity just measured; the plain form serves
+    the same requests with the same arrivals, one at a time."""
+    from rk_gb300 import serving, workloads
+    reqs = workloads.served_requests(20000, seed=7)[:count]
+    work = 0.0
+    for r in reqs:
+        if r["kind"] == "bruss":
+            work += workloads.estimated_work(dict(grid_n=r["grid_n"], alpha=2e-3))
+        else:
+            work += r["n"] * 40.0
+    scale = work / capacity / (load * reqs[-1]["arrival"])
+    loop = serving.ServingLoop(8 << 30, max_instances=4096, sweeps_per_launch=16)
+    clocks = ClockSampler(0)
+    clocks.start()
+    try:
+        o = loop.serve(reqs, time_scale=scale)
+    finally:
+        loop.close()
+    clk = clocks.stop()
+    pl = serving.serve_plain(reqs, time_scale=scale)
+    return {
+        "metric": "served solves/s and p50/p99 latency", "offered_load": load,
+        "value": o["solves_per_s"], "unit": "solves/s",
+        "latency_s": {"p50": o["p50"], "p99": o["p99"], "max": float(np.max(o["latency"]))},
+        "plain_form": {"value": pl["solves_per_s"], "unit": "solves/s", "p50": pl["p50"], "p99": pl["p99"],
+                       "sample": "the same requests and arrivals, one at a time, first come first served"},
+        "config": {"workload": f"served: first {len(reqs)} of the 20,000 seeded requests (seed 7), "
+                               f"{100.0 * len(reqs) / 20000:.1f} % of the stream",
+                   "arrival_time_scale": scale, "arena_gb": 8, "sweeps_per_launch": 16},
+        "admission_refusals": o["refusals"], "makespan_s": o["makespan"], "clocks": clk,
+    }
 
 
 MIXED_CHECK_TE = 0.004
@@ -594,6 +862,12 @@ def main():
                     help="exact (default): bit-identical to the reference; fma: fewer FP64 "
                          "instructions; mixed: FP32 stage vectors (the N=4000 configuration)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the batched, served and mixed-precision records of the default run")
+    ap.add_argument("--batched-sample", type=int, default=128,
+                    help="instances of the 4096-instance list in the default run's batched record")
+    ap.add_argument("--served-requests", type=int, default=200,
+                    help="requests of the 20,000-request stream per load in the served record")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

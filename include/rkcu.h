@@ -88,7 +88,11 @@ typedef struct
   int schedule;         /* plain form, stage synchronisation: 0 = automatic (neighbour
                            flags), 1 = grid barrier after every stage, 2 = neighbour
                            progress flags, 3 = dataflow over (stage, tile) in wavefront
-                           order; mixed form: 1 = tiles with plain loads, else TMA;
+                           order; mixed form: 0 = automatic (3 where it runs: even
+                           N, at most 8 stages; else 2), 1 = one stage at a time
+                           over tiles with plain loads, 2 = the same with TMA-staged
+                           tiles, 3 = all FP32 stages of a step per tile in shared
+                           memory;
                            low-storage form: 1 = grid barrier after every wavefront
                            step, else neighbour progress flags */
   int flow_skew;        /* schedule 3: tiles by which stage i trails stage i-1 in the
@@ -231,8 +235,12 @@ int rkcu_debug_inject_wait_timeout(rkcu_solver *s, int extra_arrivals);
    footprint (rkcu_batch_footprint) fits, and returns RKCU_ERR_NOMEM without
    side effects otherwise, so a serving loop can queue it and retry after
    finished instances are taken.  Arithmetic per instance is the exact (or
-   FMA) FP64 step loop with the correctly rounded step-size pow; an instance's
-   result does not depend on which other instances share the batch. */
+   FMA) FP64 step loop of rkcu_solve, step sizes included: a step-size factor
+   within 0.03 ulp of a rounding boundary is posted to the host, which answers
+   with the C library's pow while the launch runs (the instance sits out the
+   sweeps until the answer is there), so in the exact mode every instance
+   reproduces the reference bit for bit; an instance's result does not depend
+   on which other instances share the batch. */
 typedef struct rkcu_batch rkcu_batch;
 
 long long rkcu_batch_footprint(const rkcu_problem *prob, int stages);
@@ -243,8 +251,10 @@ int rkcu_batch_destroy(rkcu_batch *b);
    receives its slot.  RKCU_ERR_NOMEM: no room (arena or slots) right now. */
 int rkcu_batch_add(rkcu_batch *b, const rkcu_problem *prob, double t0, double te, double tol,
                    const double *y0, long long host_id, int *slot);
-/* Run up to max_sweeps sweeps (one launch, replayed from a CUDA graph);
-   *active_left receives the number of instances still integrating. */
+/* Run up to max_sweeps sweeps (one launch, replayed from a CUDA graph) and
+   wait for them; the calling thread answers posted step-size updates
+   meanwhile.  *active_left receives the number of instances still
+   integrating. */
 int rkcu_batch_run(rkcu_batch *b, int max_sweeps, int *active_left);
 /* Slots that finished since the last call (up to capacity). */
 int rkcu_batch_finished(rkcu_batch *b, int *slots, int capacity, int *count);
@@ -270,9 +280,10 @@ void *rkcu_batch_stream(rkcu_batch *b);
    BRUSS2D-MIX or LV pairs with a built-in tableau (method name), reading y0
    from and writing y to the caller's DEVICE buffers (n doubles each), and calls
    no cudaMalloc, cudaFree or other allocating routine: every piece of scratch
-   (state vectors, stage vectors, step-control state) lives in one 8 MiB + 256 B
-   static device array that each GPU loading the library holds until the process
-   exits.  Limit: n <= 65536 components (e.g. BRUSS2D-MIX up to N = 181);
+   (state vectors, stage vectors, step-control state) lives in one static device
+   array of 8 MiB + 8.25 KiB (16 vectors of 32768 double pairs, 256 B of state,
+   8 KiB of per-CTA progress words) that each GPU loading the library holds
+   until the process exits.  Limit: n <= 65536 components (e.g. BRUSS2D-MIX up to N = 181);
    larger systems return RKCU_ERR_TOO_LARGE.  The first call on a device looks up
    the array's device address (once per device, with that device current); make
    that first call before any stream capture.  All calls share the one array, so

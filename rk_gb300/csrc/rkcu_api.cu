@@ -19,12 +19,28 @@ using rkcu::kMaxStages;
 
 namespace {
 
+// Text behind rkcu_last_cuda_error(), per host thread.
 thread_local char g_cuda_err[256] = "";
 
 int cuda_fail(cudaError_t e, const char *what) {
   std::snprintf(g_cuda_err, sizeof(g_cuda_err), "%s: %s", what, cudaGetErrorString(e));
   return e == cudaErrorMemoryAllocation ? RKCU_ERR_NOMEM : RKCU_ERR_CUDA;
 }
+
+}  // namespace
+
+namespace rkcu {
+
+int record_cuda_error(cudaError_t e, const char *what) { return cuda_fail(e, what); }
+
+int record_wait_timeout(int site) {
+  std::snprintf(g_cuda_err, sizeof(g_cuda_err), "device wait timed out at site %d", site);
+  return RKCU_ERR_TIMEOUT;
+}
+
+}  // namespace rkcu
+
+namespace {
 
 #define RKCU_CK(call)                                  \
   do {                                                 \
@@ -347,6 +363,16 @@ int rkcu_set_method_by_name(rkcu_solver *s, const char *name) {
   return rkcu_set_method(s, rows, b, bh, c, st, ord);
 }
 
+// How the mixed form runs its FP32 stages: schedule 0 (automatic) and 3 all
+// stages per tile in shared memory where that path exists (even N, s <= 8),
+// else one stage at a time over TMA-staged tiles; 1 tiles with plain loads;
+// 2 TMA-staged tiles.
+static int mixed_path(const rkcu_solver *s) {
+  if (s->opt.schedule == 1) return rkcu::kMixTiles;
+  if (s->opt.schedule == 2) return rkcu::kMixTilesTma;
+  return rkcu::mixed_fused_available(s->prob.grid_n, s->s) ? rkcu::kMixFused : rkcu::kMixTilesTma;
+}
+
 int rkcu_begin(rkcu_solver *s, double t0, double te, const double *y0, int y0_on_device,
                double tol) {
   if (!s || !y0 || !s->have_method) return s ? RKCU_ERR_STATE : RKCU_ERR_INVALID;
@@ -355,7 +381,8 @@ int rkcu_begin(rkcu_solver *s, double t0, double te, const double *y0, int y0_on
   if (s->prob.problem == RKCU_PROBLEM_RHS && !s->rhs) return RKCU_ERR_STATE;
   RKCU_CK(cudaSetDevice(s->opt.device));
   if (s->opt.precision == RKCU_MIXED) {
-    const int mneed = s->s;  // f0, y32, dF[1..s-2]
+    // f0, y32 and, unless all FP32 stages run per tile in shared memory, dF[1..s-2]
+    const int mneed = mixed_path(s) == rkcu::kMixFused ? 2 : s->s;
     if (s->mstage_vectors < mneed) {
       if (s->mstage) {
         RKCU_CK(cudaStreamSynchronize(s->stream));
@@ -518,14 +545,14 @@ int rkcu_advance(rkcu_solver *s, int max_steps) {
     const size_t np = s->npairs;
     m.f0 = s->mstage;
     m.y32 = s->mstage + np;
-    for (int j = 1; j <= s->s - 2; ++j) m.dF[j] = s->mstage + (size_t)(1 + j) * np;
+    // the dF vectors exist unless the FP32 stages run per tile in shared memory
+    if (s->mstage_vectors >= s->s)
+      for (int j = 1; j <= s->s - 2; ++j) m.dF[j] = s->mstage + (size_t)(1 + j) * np;
     m.st = s->st;
     m.bruss.N = s->prob.grid_n;
     m.bruss.coef = bruss_coef(&s->prob);
     int grid = 0;
-    // FP32 stage tiles staged through TMA (even N, s <= 8; else plain loads);
-    // schedule 1 keeps the plain loads
-    const int path = s->opt.schedule == 1 ? rkcu::kMixTiles : rkcu::kMixTilesTma;
+    const int path = mixed_path(s);
     cudaError_t e = rkcu::launch_mixed(m, path, s->num_sms, s->stream, &grid);
     if (e != cudaSuccess) return cuda_fail(e, "mixed kernel launch");
     s->last_grid = grid;
@@ -622,11 +649,7 @@ int rkcu_query(rkcu_solver *s, rkcu_stats *stats) {
         s->opt.step_limit > 0 && h->steps_acc + h->steps_rej >= s->opt.step_limit;
     stats->host_pow_steps = h->host_pow_steps;
   }
-  if (h->error) {
-    std::snprintf(g_cuda_err, sizeof(g_cuda_err), "device wait timed out at site %d",
-                  h->error_site);
-    return RKCU_ERR_TIMEOUT;
-  }
+  if (h->error) return rkcu::record_wait_timeout(h->error_site);
   return RKCU_OK;
 }
 

@@ -9,7 +9,12 @@
 //            each stage
 //   error    per-chunk block reduction, 64-bit atomicMax into the instance
 //   control  one thread per instance: accept/reject, step size (correctly
-//            rounded pow), t, counters, next h*A (include/tools.h:191-278)
+//            rounded pow), t, counters, next h*A (include/tools.h:191-278);
+//            a factor within 0.03 ulp of a rounding boundary is posted to the
+//            host, which answers with the C library's pow while the kernel
+//            runs (mapped host memory); the instance sits out the sweeps
+//            until the answer is there, so every instance takes the
+//            reference's step sizes
 //   compact  when an instance finished, CTA 0 rebuilds the chunk list; the
 //            chunk length is the tuned one, shortened when the active pairs
 //            would give fewer than two chunks per CTA (a few large instances)
@@ -19,6 +24,16 @@
 #include "rkcu_batch.cuh"
 
 namespace rkcu {
+
+// System-scope release store / acquire load of a word in mapped host memory.
+__device__ __forceinline__ void st_release_sys(unsigned int *p, unsigned int v) {
+  asm volatile("st.release.sys.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned int ld_acquire_sys(const unsigned int *p) {
+  unsigned int v;
+  asm volatile("ld.acquire.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
 
 template <int kExact>
 __device__ __forceinline__ double2 batch_rhs(const InstDesc &d, const double2 *w, int p) {
@@ -119,6 +134,7 @@ __global__ void __launch_bounds__(kT, batch_threads_per_sm<kExact>() / kT) batch
       for (int c = blockIdx.x; c < nch; c += gridDim.x) {
         const int2 ch = P.chunks[c];
         const InstDesc &d = P.desc[ch.x];
+        if (d.pending) continue;  // waits for its step size from the host (same for every CTA)
         const InstCoef &K = P.coef[ch.x];
         const size_t np = static_cast<size_t>(d.npairs);
         double2 *__restrict__ vec = d.vec;
@@ -204,23 +220,45 @@ __global__ void __launch_bounds__(kT, batch_threads_per_sm<kExact>() / kT) batch
     for (int slot = gtid; slot < nslots; slot += gstride) {
       InstDesc &d = P.desc[slot];
       if (!d.active || d.done) continue;
-      const double errmax = __longlong_as_double((long long)d.errbits);
       double t = d.t, hh = d.h;
-      if (d.tol <= 0.0) {
-        t += hh;
-        ++d.steps_acc;
-        d.cur ^= 1;
+      if (d.pending) {
+        // the host's step size (tools.h:221-233 with the C library's pow), once posted
+        PowBox *box = P.pow_box + slot;
+        if (ld_acquire_sys(&box->ans) != d.pend_seq) continue;
+        hh = *(volatile double *)&box->h_new;
+        d.pending = 0;
       } else {
-        bool host_pow;  // batched instances keep the correctly rounded factor
-        const double hn = h_new(hh, errmax, d.tol, P.ord, &host_pow);
-        if (errmax <= d.tol) {
+        const double errmax = __longlong_as_double((long long)d.errbits);
+        if (d.tol <= 0.0) {
           t += hh;
           ++d.steps_acc;
           d.cur ^= 1;
         } else {
-          ++d.steps_rej;
+          bool host_pow;
+          const double hn = h_new(hh, errmax, d.tol, P.ord, &host_pow);
+          if (errmax <= d.tol) {
+            t += hh;
+            ++d.steps_acc;
+            d.cur ^= 1;
+          } else {
+            ++d.steps_rej;
+          }
+          if (host_pow) {
+            // within 0.03 ulp of a rounding boundary the C library's pow, which the
+            // reference uses, may round the other way: post the update to the host
+            // and sit out the sweeps until its answer arrives
+            PowBox *box = P.pow_box + slot;
+            d.t = t;
+            d.errbits = 0ull;
+            d.pending = 1;
+            d.pend_seq = d.pend_seq + 1;
+            *(volatile double *)&box->err = errmax;
+            *(volatile double *)&box->h = hh;
+            st_release_sys(&box->req, d.pend_seq);
+            continue;
+          }
+          hh = hn;
         }
-        hh = hn;
       }
       hh = fmin(hh, d.te - t);
       d.t = t;

@@ -19,6 +19,21 @@ struct InstDesc {
   int steps_acc, steps_rej, cur, done, active, step_limit;
   long long host_id;            // caller's id, returned with the result
   unsigned long long errbits;   // error max of the running step (bit pattern, >= 0)
+  // A step whose size update waits for the C library's pow on the host (the
+  // accept/reject decision, t and the counters are applied): the instance sits
+  // out the sweeps until the host's answer with sequence number pend_seq is in
+  // its PowBox.
+  int pending;
+  unsigned int pend_seq;
+};
+
+// Mailbox of one slot in mapped, pinned host memory: the kernel posts the
+// error max and step size of a step whose size update is left to the host
+// (req = sequence number, written last with release semantics); the host
+// answers with the new step size (ans = req, written last).
+struct PowBox {
+  unsigned int req, ans;
+  double err, h, h_new;
 };
 
 // h*A, h*b, h*(b - b^) of the running step, one per slot (device memory)
@@ -47,6 +62,7 @@ struct BatchParams {
   int nblocks;
   unsigned long long timeout_ns;
   DevState *st;        // barrier words and error flag
+  PowBox *pow_box;     // one mailbox per slot (device view of mapped host memory)
 };
 
 cudaError_t launch_batch_rebuild(const BatchParams &p, cudaStream_t stream);

@@ -31,6 +31,8 @@ struct SlotInfo {
   size_t off = 0, size = 0;
   int n = 0, npairs = 0;
   long long host_id = -1;
+  double tol = 0.0;
+  long long host_pow = 0;  // step-size updates answered by the host
 };
 
 size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
@@ -52,6 +54,8 @@ struct rkcu_batch {
   int *d_ints = nullptr;  // [0] nslots, [1] nchunks, [2] rebuild, [3] done_count, [4] chunk length
   int *d_done = nullptr;
   DevState *d_st = nullptr;
+  rkcu::PowBox *h_box = nullptr;  // mapped, pinned host memory: one mailbox per slot
+  rkcu::PowBox *d_box = nullptr;  // its device address
   char *arena = nullptr;
   size_t arena_bytes = 0;
   std::vector<FreeBlock> free_list;
@@ -142,7 +146,38 @@ BatchParams make_params(rkcu_batch *b, int budget) {
   p.budget = budget;
   p.timeout_ns = (unsigned long long)(b->opt.wait_timeout_s * 1e9);
   p.st = b->d_st;
+  p.pow_box = b->d_box;
   return p;
+}
+
+// Answer the step-size updates the kernel posted: include/tools.h:221-233 with
+// the C library's pow, as the reference computes every update.
+void serve(rkcu_batch *b) {
+  for (int i = 0; i < b->nslots_high; ++i) {
+    SlotInfo &si = b->slots[i];
+    if (si.state != 1) continue;
+    rkcu::PowBox &x = b->h_box[i];
+    const unsigned req = __atomic_load_n(&x.req, __ATOMIC_ACQUIRE);
+    if (req == x.ans) continue;  // nothing new (only the host writes ans)
+    const double err = x.err, h = x.h;
+    x.h_new = h * std::fmin(2.0, std::fmax(0.5, 0.9 * std::pow(si.tol / err, 1.0 / (b->ord + 1.0))));
+    __atomic_store_n(&x.ans, req, __ATOMIC_RELEASE);
+    ++si.host_pow;
+  }
+}
+
+// Wait for the batch's stream, answering posted step-size updates meanwhile
+// (the kernel never waits for an answer: an instance with an update pending
+// sits out the sweeps until the answer is there).
+int wait_serving(rkcu_batch *b) {
+  for (;;) {
+    serve(b);
+    const cudaError_t q = cudaStreamQuery(b->stream);
+    if (q == cudaSuccess) break;
+    if (q != cudaErrorNotReady) return fail(b, q, "batch launch");
+  }
+  serve(b);
+  return RKCU_OK;
 }
 
 void drop_graph(rkcu_batch *b) {
@@ -298,6 +333,12 @@ int rkcu_batch_create(rkcu_batch **out, long long arena_bytes, int max_instances
     return bail(fail(b, e, "done list"));
   if ((e = cudaMalloc(&b->d_st, sizeof(DevState))) != cudaSuccess) return bail(fail(b, e, "state"));
   if ((e = cudaMemset(b->d_st, 0, sizeof(DevState))) != cudaSuccess) return bail(fail(b, e, "state"));
+  if ((e = cudaHostAlloc(&b->h_box, sizeof(rkcu::PowBox) * max_instances,
+                         cudaHostAllocMapped | cudaHostAllocPortable)) != cudaSuccess)
+    return bail(fail(b, e, "step-size mailboxes"));
+  std::memset(b->h_box, 0, sizeof(rkcu::PowBox) * max_instances);
+  if ((e = cudaHostGetDevicePointer(&b->d_box, b->h_box, 0)) != cudaSuccess)
+    return bail(fail(b, e, "step-size mailboxes"));
   *out = b;
   return RKCU_OK;
 }
@@ -314,6 +355,7 @@ int rkcu_batch_destroy(rkcu_batch *b) {
   cudaFree(b->d_ints);
   cudaFree(b->d_done);
   cudaFree(b->d_st);
+  if (b->h_box) cudaFreeHost(b->h_box);
   if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return RKCU_OK;
@@ -385,6 +427,7 @@ int rkcu_batch_add(rkcu_batch *b, const rkcu_problem *prob, double t0, double te
     k.hb[r] = d.h * b->b[r];
     k.hbh[r] = d.h * b->bh[r];
   }
+  b->h_box[slot] = rkcu::PowBox{};  // no request outstanding (d.pend_seq = 0)
   BCK(cudaMemcpyAsync(b->d_desc + slot, &d, sizeof(d), cudaMemcpyHostToDevice, b->stream));
   BCK(cudaMemcpyAsync(b->d_coef + slot, &k, sizeof(k), cudaMemcpyHostToDevice, b->stream));
   if (slot + 1 > b->nslots_high) {
@@ -399,6 +442,8 @@ int rkcu_batch_add(rkcu_batch *b, const rkcu_problem *prob, double t0, double te
   si.n = prob->n;
   si.npairs = (int)np;
   si.host_id = host_id;
+  si.tol = tol;
+  si.host_pow = 0;
   if (d.done)
     b->finished.push_back(slot);
   else
@@ -413,6 +458,7 @@ int rkcu_batch_run(rkcu_batch *b, int max_sweeps, int *active_left) {
   if (b->active > 0) {
     int rc = launch(b, max_sweeps);
     if (rc != RKCU_OK) return rc;
+    if ((rc = wait_serving(b)) != RKCU_OK) return rc;
     if ((rc = collect(b)) != RKCU_OK) return rc;
   }
   if (active_left) *active_left = b->active;
@@ -451,7 +497,7 @@ int rkcu_batch_take(rkcu_batch *b, int slot, double *y, rkcu_stats *stats, long 
     stats->h = d.h;
     stats->done = d.done;
     stats->step_limit_reached = d.step_limit > 0 && d.steps_acc + d.steps_rej >= d.step_limit;
-    stats->host_pow_steps = 0;
+    stats->host_pow_steps = si.host_pow;
   }
   if (host_id) *host_id = si.host_id;
   arena_free(b, si.off, si.size);
@@ -510,6 +556,7 @@ int rkcu_batch_tune(rkcu_batch *b, int sweeps_per_trial, double *best_ns_per_pai
         int rc = launch(b, sweeps_per_trial);
         if (rc != RKCU_OK) return rc;
         BCK(cudaEventRecord(e1, b->stream));
+        if ((rc = wait_serving(b)) != RKCU_OK) return rc;
         BCK(cudaEventSynchronize(e1));
         float ms = 0.f;
         BCK(cudaEventElapsedTime(&ms, e0, e1));

@@ -116,6 +116,91 @@ __device__ __forceinline__ float2 delta_at(const float2 *const *jp, const float 
   return make_float2(fmaf(hc, f.x, acc.x), fmaf(hc, f.y, acc.y));
 }
 
+// Coefficients of the update at one grid point, per step (shared memory):
+// h b_j and h (b_j - b^_j) as FP32 (hb) and as double-float pairs (hbh_hi/lo).
+struct MixCoef {
+  float hb[kMaxStages], hbh_hi[kMaxStages], hbh_lo[kMaxStages];
+  float hbhs_hi, hbhs_lo;  // h sum_j (b_j - b^_j), the F0 term of the estimate
+};
+
+// h c x + lo as a double-float product of the pair (c_hi, c_lo) with the float
+// x: the leading product exact (TwoProduct), the low part's product rounded.
+__device__ __forceinline__ dfl::df df_term(float c_hi, float c_lo, float x) {
+  const dfl::df p = dfl::two_prod(c_hi, x);
+  return {p.hi, dfl::f_fma(c_lo, x, p.lo)};
+}
+
+// The step's update at one grid point from its stage increments d[1..s-2]
+// and dlast (dF_1 .. dF_{s-1}) and F0 (f):
+//   dY = sum_j h b_j dF_j     FP32, Kahan-compensated, in stage order
+//   y_new = y1 + dY           FP64 (y1 = y + h sum(b) F0 from stage 0)
+//   e = h sum(b - b^) F0 + sum_j h (b_j - b^_j) dF_j
+//                             double-float: every product to about 2^-47, the
+//                             sum to about 2^-44 relative, in stage order
+// and the error ratios |e| / max(|y_new|, |y|) of the pair's two components
+// (FP32 from the estimate's leading part; a zero divisor gives 3e38, so the
+// step is rejected, as the reference's 1.7e308 of include/tools.h:284 would).
+template <int kMaxS>
+__device__ __forceinline__ double2 mix_update(const float2 (&d)[kMaxS], float2 dlast, int s, float2 f,
+                                              float2 y32, double2 y1, const MixCoef &c, float *rx,
+                                              float *ry) {
+  float2 sum = make_float2(0.f, 0.f), cmp = make_float2(0.f, 0.f);
+  dfl::df ex = df_term(c.hbhs_hi, c.hbhs_lo, f.x), ey = df_term(c.hbhs_hi, c.hbhs_lo, f.y);
+#pragma unroll
+  for (int jj = 1; jj < kMaxS; ++jj) {
+    if (jj >= s) break;
+    const float2 dj = jj == s - 1 ? dlast : d[jj];
+    const float ax = fmaf(c.hb[jj], dj.x, -cmp.x), ay = fmaf(c.hb[jj], dj.y, -cmp.y);
+    const float tx = sum.x + ax, ty = sum.y + ay;
+    cmp.x = (tx - sum.x) - ax;
+    cmp.y = (ty - sum.y) - ay;
+    sum.x = tx;
+    sum.y = ty;
+    ex = dfl::df_add(ex, df_term(c.hbh_hi[jj], c.hbh_lo[jj], dj.x));
+    ey = dfl::df_add(ey, df_term(c.hbh_hi[jj], c.hbh_lo[jj], dj.y));
+  }
+  const double2 yn = make_double2(__dadd_rn(y1.x, dfl::dbl_of(sum.x - cmp.x)),
+                                  __dadd_rn(y1.y, dfl::dbl_of(sum.y - cmp.y)));
+  const float dnx = fmaxf(fabsf(trunc_to_float(yn.x)), fabsf(y32.x));
+  const float dny = fmaxf(fabsf(trunc_to_float(yn.y)), fabsf(y32.y));
+  const float erx = ex.hi + ex.lo, ery = ey.hi + ey.lo;
+  *rx = dnx == 0.0f ? 3.0e38f : fabsf(erx) / dnx;
+  *ry = dny == 0.0f ? 3.0e38f : fabsf(ery) / dny;
+  return yn;
+}
+
+// Fused FP32 stages: all stages 1 .. s-1 of a step on one tile of kFT x kFT
+// grid points in shared memory.  Stage i is evaluated on the tile and a halo
+// of s-1-i points (its increments are read one point further out by the next
+// stage's stencil), so the last stage needs the tile alone; only F0 and y32
+// (with a halo of s-1 points) are read from memory, one TMA box each,
+// double-buffered, and only y_new is written.
+constexpr int kFT = 32;
+constexpr int kFusedThreads = 512;
+constexpr int mix_threads(int path) { return path == kMixFused ? kFusedThreads : kMixThreads; }
+
+template <int kS>
+struct FusedGeom {
+  static constexpr int HY = kS - 1;                       // row halo
+  static constexpr int HX = (kS - 1 + 1) / 2 * 2;         // column halo, even: a TMA box
+                                                          // must start on 16 bytes
+  static constexpr int FR = kFT + 2 * HY, FC = kFT + 2 * HX;  // frame rows, columns
+  static constexpr int kFrame = FR * FC;                  // points (float2) per frame
+  static constexpr unsigned kFrameBytes = (kFrame * 8u + 127u) / 128u * 128u;
+  // F0 and y32 twice (double buffer), delta, dF_1 .. dF_{s-2}
+  static constexpr int kFrames = 5 + (kS > 2 ? kS - 2 : 0);
+  static constexpr size_t kSmem = static_cast<size_t>(kFrames) * kFrameBytes + 128;
+  static_assert(2 * FC <= 256 && FR <= 256, "TMA box dimensions are at most 256 elements");
+};
+
+template <int kFirst, int kLast, class F>
+__device__ __forceinline__ void static_for(F &&f) {
+  if constexpr (kFirst < kLast) {
+    f(std::integral_constant<int, kFirst>{});
+    static_for<kFirst + 1, kLast>(f);
+  }
+}
+
 // Stage 0 at one pair in FP64 (fused, products in software binary64): the
 // path for points whose values the double-float evaluation does not cover.
 // Out of line, so that its FP64 instructions are not if-converted into the
@@ -132,7 +217,7 @@ static __device__ __noinline__ void stage0_point_fp64(const Bruss &br, const dou
 // kMaxS: an upper bound of the stage count (8 or 13), so that the per-stage
 // loops over earlier stages unroll; kPath: how the FP32 stages walk the grid.
 template <int kMaxS, int kPath>
-__global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
+__global__ void __launch_bounds__(mix_threads(kPath), kPath == kMixFused ? 1 : (kMaxS <= 8 ? 4 : 2))
     mixed_kernel(const __grid_constant__ MixedParams P) {
   // TMA staging buffers: 2 (double buffer) x s slots of kSlotBytes, from the
   // first 128-byte boundary of the dynamic shared memory (128 bytes spare)
@@ -142,8 +227,10 @@ __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
   __shared__ double s_t, s_h;
   __shared__ int s_acc, s_rej, s_cur, s_done;
   __shared__ unsigned long long s_step;
-  __shared__ double s_wmax[kMixThreads / 32];
-  __shared__ float hb[kMaxStages], hbh[kMaxStages], hc[kMaxStages];
+  constexpr int kT = mix_threads(kPath);
+  __shared__ double s_wmax[kT / 32];
+  __shared__ float hb[kMaxStages], hc[kMaxStages];
+  __shared__ MixCoef s_coef;
   // per stage i: the j < i with a_ij != 0 (j = 1 always, as the running sums
   // of the scatter order start there) and h a_ij, for the gather
   __shared__ const float2 *s_jp[kMaxStages][kMaxStages];
@@ -152,7 +239,6 @@ __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
   __shared__ int s_nj[kMaxStages];
   __shared__ double s_hbsum;
   __shared__ float s_hbs_hi, s_hbs_lo;  // h sum(b) as a double-float pair
-  __shared__ float s_hbhsum;
   __shared__ float2 s_delta[kTileR + 2][kTileC + 2];  // delta_i on a tile and its halo
 
   DevState *st = P.st;
@@ -173,7 +259,7 @@ __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
     s_done = st->done;
     s_step = st->step;
   }
-  if (threadIdx.x == 0 && kPath == kMixTilesTma) {
+  if (threadIdx.x == 0 && (kPath == kMixTilesTma || kPath == kMixFused)) {
     mbar_init(&s_mbar[0], 1);
     mbar_init(&s_mbar[1], 1);
     mbar_fence_init();
@@ -199,15 +285,21 @@ __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
       s_nj[i] = nj;
     }
     if (threadIdx.x < kMaxStages) {
-      hb[threadIdx.x] = static_cast<float>(h * P.b[threadIdx.x]);
-      hbh[threadIdx.x] = static_cast<float>(h * P.bh[threadIdx.x]);
-      hc[threadIdx.x] = static_cast<float>(h * P.csum[threadIdx.x]);
+      const int j = threadIdx.x;
+      hb[j] = static_cast<float>(h * P.b[j]);
+      hc[j] = static_cast<float>(h * P.csum[j]);
+      const double hbh = h * P.bh[j];
+      s_coef.hb[j] = hb[j];
+      s_coef.hbh_hi[j] = static_cast<float>(hbh);
+      s_coef.hbh_lo[j] = static_cast<float>(hbh - static_cast<double>(s_coef.hbh_hi[j]));
     }
     if (threadIdx.x == 0) {
       s_hbsum = h * P.bsum;
       s_hbs_hi = static_cast<float>(s_hbsum);
       s_hbs_lo = static_cast<float>(s_hbsum - static_cast<double>(s_hbs_hi));
-      s_hbhsum = static_cast<float>(h * P.bhsum);
+      const double hbhs = h * P.bhsum;
+      s_coef.hbhs_hi = static_cast<float>(hbhs);
+      s_coef.hbhs_lo = static_cast<float>(hbhs - static_cast<double>(s_coef.hbhs_hi));
     }
     __syncthreads();
     const double2 *__restrict__ ycur = P.y[s_cur];
@@ -246,11 +338,113 @@ __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
         P.y32[p] = make_float2(trunc_to_float(c.x), trunc_to_float(c.y));
       }
     }
-    if (kPath == kMixTilesTma) fence_proxy_async_global();  // f0, y32 are read by TMA next
+    if (kPath == kMixTilesTma || kPath == kMixFused) fence_proxy_async_global();  // f0, y32 are read by TMA next
     if (!(ok = grid_barrier(st, P.nblocks, P.timeout_ns, 11))) break;
 
     float emax = 0.0f;
     const int N = br.N;
+    if constexpr (kPath == kMixFused) {
+      // All FP32 stages per tile (FusedGeom): F0 and y32 frames through TMA,
+      // double-buffered; delta_i and dF_i in shared-memory frames.
+      using G = FusedGeom<kMaxS>;
+      auto frame = [&](int f) { return reinterpret_cast<float2 *>(s_box + static_cast<size_t>(f) * G::kFrameBytes); };
+      const int tiles_x = (N + kFT - 1) / kFT;
+      const int ntiles = tiles_x * tiles_x;
+      float2 *const fd = frame(4);
+      auto issue = [&](int t, int b) {
+        const int k0 = (t / tiles_x) * kFT, j0 = (t % tiles_x) * kFT;
+        mbar_arrive_expect_tx(&s_mbar[b], 2u * G::kFrame * 8u);
+        tma_load_2d(frame(2 * b), &P.tm[0], 2 * (j0 - G::HX), k0 - G::HY, &s_mbar[b]);
+        tma_load_2d(frame(2 * b + 1), &P.tm[1], 2 * (j0 - G::HX), k0 - G::HY, &s_mbar[b]);
+      };
+      int b = 0;
+      __syncthreads();  // the frames are free (the previous step is done with them)
+      if (blockIdx.x < ntiles) {
+        if (threadIdx.x == 0) issue(blockIdx.x, 0);
+        pending |= 1u;
+      }
+      // A thread whose wait ran out of time skips the tile's work; the CTA
+      // agrees on it at the next tile's first barrier (the solve then ends
+      // with the error set).
+      bool bad = false;
+      for (int t = blockIdx.x; t < ntiles; t += gridDim.x, b ^= 1) {
+        const int tn = t + gridDim.x;
+        if (__syncthreads_or(bad)) break;  // buffer b^1, delta and the dF frames are free
+        if (tn < ntiles) {
+          if (threadIdx.x == 0) issue(tn, b ^ 1);
+          pending |= 2u >> b;  // bit of buffer b^1
+        }
+        const bool got = mbar_wait(&s_mbar[b], (phase >> b) & 1u, st, P.timeout_ns, 16);
+        bad = bad || !got;
+        if (got) {
+          phase ^= 1u << b;
+          pending &= ~(1u << b);
+        }
+        const int k0 = (t / tiles_x) * kFT, j0 = (t % tiles_x) * kFT;
+        const float2 *const ff0 = frame(2 * b), *const fy32 = frame(2 * b + 1);
+        static_for<1, kMaxS>([&](auto ic) {
+          constexpr int i = decltype(ic)::value;
+          // delta_i on the tile and a halo of s-i points (frame rows/columns
+          // HY-dd.., HX-dd..); points outside the grid are never read
+          constexpr int dd = kMaxS - i, RD = kFT + 2 * dd;
+          const int nj = s_nj[i];
+          const float hci = hc[i];
+          for (int idx = threadIdx.x; got && idx < RD * RD; idx += kFusedThreads) {
+            const int r = idx / RD, c = idx - (idx / RD) * RD;
+            const int k = k0 - dd + r, j = j0 - dd + c;
+            if (static_cast<unsigned>(k) >= static_cast<unsigned>(N) ||
+                static_cast<unsigned>(j) >= static_cast<unsigned>(N))
+              continue;
+            const int e = (G::HY - dd + r) * G::FC + (G::HX - dd + c);
+            float2 acc = make_float2(0.0f, 0.0f);
+#pragma unroll
+            for (int kk = 0; kk < (i > 1 ? i - 1 : 1); ++kk) {
+              if (kk < nj) {
+                const float a = s_ja[i][kk];
+                const float2 d = frame(4 + s_jl[i][kk])[e];
+                acc.x = fmaf(a, d.x, acc.x);
+                acc.y = fmaf(a, d.y, acc.y);
+              }
+            }
+            const float2 f = ff0[e];
+            fd[e] = make_float2(fmaf(hci, f.x, acc.x), fmaf(hci, f.y, acc.y));
+          }
+          __syncthreads();
+          // dF_i on the tile and a halo of s-1-i points
+          constexpr int dq = kMaxS - 1 - i, RQ = kFT + 2 * dq;
+          for (int idx = threadIdx.x; got && idx < RQ * RQ; idx += kFusedThreads) {
+            const int r = idx / RQ, c = idx - (idx / RQ) * RQ;
+            const int k = k0 - dq + r, j = j0 - dq + c;
+            if (static_cast<unsigned>(k) >= static_cast<unsigned>(N) ||
+                static_cast<unsigned>(j) >= static_cast<unsigned>(N))
+              continue;
+            const int e = (G::HY - dq + r) * G::FC + (G::HX - dq + c);
+            // a boundary row or column uses its inner neighbour twice
+            const int eu = k == 0 ? e + G::FC : e - G::FC;
+            const int en = k == N - 1 ? e - G::FC : e + G::FC;
+            const int jcase = j == 0 ? 1 : (j == N - 1 ? 2 : 0);
+            const float2 dF = delta_rhs(fd[e], fd[eu], fd[en], fd[e - 1], fd[e + 1], jcase, fy32[e], coef);
+            if constexpr (i < kMaxS - 1) {
+              frame(4 + i)[e] = dF;
+            } else {
+              // the last stage: the update and the error ratio at the tile's point
+              float2 dall[kMaxS];
+              dall[0] = make_float2(0.f, 0.f);
+#pragma unroll
+              for (int jj = 1; jj < kMaxS - 1; ++jj) dall[jj] = frame(4 + jj)[e];
+              const size_t p = static_cast<size_t>(k) * N + j;
+              float rx, ry;
+              ynew[p] = mix_update<kMaxS>(dall, dF, kMaxS, ff0[e], fy32[e], ynew[p], s_coef, &rx, &ry);
+              emax = fmaxf(emax, rx);
+              if (2 * p + 1 < static_cast<size_t>(P.n)) emax = fmaxf(emax, ry);
+            }
+          }
+          if constexpr (i < kMaxS - 1) __syncthreads();
+        });
+      }
+      if (__syncthreads_or(bad)) ok = false;
+      if (!ok) break;
+    } else {
     const int tiles_x = (N + kTileC - 1) / kTileC;
     const int ntiles = tiles_x * ((N + kTileR - 1) / kTileR);
     const int tr = threadIdx.x / kTileC, tc = threadIdx.x % kTileC;
@@ -270,35 +464,16 @@ __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
           P.dF[i][p] = dF;
           return;
         }
-        // dY (Kahan-compensated) and the error estimate, in order of the stages
-        const float2 f = own_f0();
-        float2 sum = make_float2(0.f, 0.f), cmp = make_float2(0.f, 0.f);
-        float2 er = make_float2(s_hbhsum * f.x, s_hbhsum * f.y);
-        float2 dj[kMaxS - 1];
+        // dY, y_new and the error estimate, in order of the stages
+        float2 dall[kMaxS];
+        dall[0] = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int jj = 1; jj < kMaxS - 1; ++jj)
-          if (jj < s - 1) dj[jj] = own_dF(jj);
-#pragma unroll
-        for (int jj = 1; jj < kMaxS; ++jj) {
-          if (jj >= s) break;
-          const float2 d = jj == s - 1 ? dF : dj[jj < kMaxS - 1 ? jj : 0];
-          const float ax = fmaf(hb[jj], d.x, -cmp.x), ay = fmaf(hb[jj], d.y, -cmp.y);
-          const float tx = sum.x + ax, ty = sum.y + ay;
-          cmp.x = (tx - sum.x) - ax;
-          cmp.y = (ty - sum.y) - ay;
-          sum.x = tx;
-          sum.y = ty;
-          er.x = fmaf(hbh[jj], d.x, er.x);
-          er.y = fmaf(hbh[jj], d.y, er.y);
-        }
-        const double2 y1 = own_y1();
-        const double2 yn = make_double2(__dadd_rn(y1.x, dfl::dbl_of(sum.x - cmp.x)),
-                                        __dadd_rn(y1.y, dfl::dbl_of(sum.y - cmp.y)));
-        ynew[p] = yn;
-        const float dnx = fmaxf(fabsf(trunc_to_float(yn.x)), fabsf(y32.x));
-        const float dny = fmaxf(fabsf(trunc_to_float(yn.y)), fabsf(y32.y));
-        emax = fmaxf(emax, dnx == 0.0f ? 3.0e38f : fabsf(er.x) / dnx);
-        if (2 * p + 1 < P.n) emax = fmaxf(emax, dny == 0.0f ? 3.0e38f : fabsf(er.y) / dny);
+        for (int jj = 1; jj < kMaxS; ++jj)
+          if (jj < s - 1) dall[jj] = own_dF(jj);
+        float rx, ry;
+        ynew[p] = mix_update<kMaxS>(dall, dF, s, own_f0(), y32, own_y1(), s_coef, &rx, &ry);
+        emax = fmaxf(emax, rx);
+        if (2 * p + 1 < P.n) emax = fmaxf(emax, ry);
       };
       auto finish_point = [&](int tr_, int tc_, int k, int j, float2 y32, auto &&own_dF,
                               auto &&own_f0, auto &&own_y1) {
@@ -413,6 +588,7 @@ __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
         if (!(ok = grid_barrier(st, P.nblocks, P.timeout_ns, 12))) break;
       }
     }
+    }
     if (!ok) break;
 
     double dmax = static_cast<double>(emax);  // the norm is reduced in FP64
@@ -422,7 +598,7 @@ __global__ void __launch_bounds__(kMixThreads, kMaxS <= 8 ? 4 : 2)
     __syncthreads();
     if (threadIdx.x == 0) {
       double m = s_wmax[0];
-      for (int k = 1; k < kMixThreads / 32; ++k) m = fmax(m, s_wmax[k]);
+      for (int k = 1; k < kT / 32; ++k) m = fmax(m, s_wmax[k]);
       atomicMax(&st->err_slot[s_step & 1], (unsigned long long)__double_as_longlong(m));
     }
     if (!(ok = grid_barrier(st, P.nblocks, P.timeout_ns, 13))) break;
@@ -493,46 +669,94 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 }
 
 // 2-D map of an N x N grid of float2 pairs (rows of 2N floats) with boxes of
-// kBoxRows rows x kBoxPairs pairs; false if the layout does not allow TMA.
-static bool encode_box_map(CUtensorMap *m, const float2 *base, int N) {
+// box_rows rows x box_pairs pairs; false if the layout does not allow TMA.
+static bool encode_box_map(CUtensorMap *m, const float2 *base, int N, int box_pairs = kBoxPairs,
+                           int box_rows = kBoxRows) {
   auto fn = encode_fn();
   if (!fn || N % 2 || (reinterpret_cast<uintptr_t>(base) & 15)) return false;
   const cuuint64_t dims[2] = {2ull * N, static_cast<cuuint64_t>(N)};
   const cuuint64_t strides[1] = {8ull * N};  // bytes between rows: a multiple of 16 for even N
-  const cuuint32_t box[2] = {2u * kBoxPairs, static_cast<cuuint32_t>(kBoxRows)};
+  const cuuint32_t box[2] = {2u * static_cast<cuuint32_t>(box_pairs), static_cast<cuuint32_t>(box_rows)};
   const cuuint32_t estr[2] = {1, 1};
   return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float2 *>(base), dims, strides, box, estr,
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// The fused path's kernel, shared memory and TMA box for s stages (2..8).
+struct FusedShape {
+  const void *kern;
+  size_t smem;
+  int box_pairs, box_rows;
+};
+template <int kS>
+static FusedShape fused_shape() {
+  return {(const void *)mixed_kernel<kS, kMixFused>, FusedGeom<kS>::kSmem, FusedGeom<kS>::FC,
+          FusedGeom<kS>::FR};
+}
+static bool fused_shape_of(int s, FusedShape *out) {
+  switch (s) {
+    case 2: *out = fused_shape<2>(); return true;
+    case 3: *out = fused_shape<3>(); return true;
+    case 4: *out = fused_shape<4>(); return true;
+    case 5: *out = fused_shape<5>(); return true;
+    case 6: *out = fused_shape<6>(); return true;
+    case 7: *out = fused_shape<7>(); return true;
+    case 8: *out = fused_shape<8>(); return true;
+    default: return false;
+  }
+}
+
+bool mixed_fused_available(int N, int s) {
+  FusedShape f;
+  return encode_fn() != nullptr && N % 2 == 0 && fused_shape_of(s, &f);
+}
+
 cudaError_t launch_mixed(const MixedParams &p, int path, int num_sms, cudaStream_t stream,
                          int *grid_out) {
   MixedParams q = p;
-  q.path = path == kMixTilesTma ? kMixTiles : path;
-  if (path == kMixTilesTma && p.s <= kMixTmaStages) {
-    bool good = encode_box_map(&q.tm[0], p.f0, p.bruss.N) && encode_box_map(&q.tm[1], p.y32, p.bruss.N);
-    for (int j = 1; good && j <= p.s - 2; ++j) good = encode_box_map(&q.tm[1 + j], p.dF[j], p.bruss.N);
-    if (good) q.path = kMixTilesTma;
+  const void *kern = nullptr;
+  size_t dyn = 0;
+  int threads = kMixThreads;
+  int useful = (p.npairs + kMixThreads - 1) / kMixThreads;
+  if (path == kMixFused) {
+    // needs mixed_fused_available(N, s); the dF vectors are not allocated then
+    FusedShape f;
+    if (!fused_shape_of(p.s, &f) ||
+        !encode_box_map(&q.tm[0], p.f0, p.bruss.N, f.box_pairs, f.box_rows) ||
+        !encode_box_map(&q.tm[1], p.y32, p.bruss.N, f.box_pairs, f.box_rows))
+      return cudaErrorInvalidValue;
+    q.path = kMixFused;
+    kern = f.kern;
+    dyn = f.smem;
+    threads = kFusedThreads;
+    const int tiles_x = (p.bruss.N + kFT - 1) / kFT;
+    useful = tiles_x * tiles_x;
+  } else {
+    q.path = kMixTiles;
+    if (path == kMixTilesTma && p.s <= kMixTmaStages) {
+      bool good = encode_box_map(&q.tm[0], p.f0, p.bruss.N) && encode_box_map(&q.tm[1], p.y32, p.bruss.N);
+      for (int j = 1; good && j <= p.s - 2; ++j) good = encode_box_map(&q.tm[1 + j], p.dF[j], p.bruss.N);
+      if (good) q.path = kMixTilesTma;
+    }
+    // one instantiation per path, so that each gets its own register allocation
+    kern = p.s > 8                  ? (const void *)mixed_kernel<kMaxStages, kMixTiles>
+           : q.path == kMixTilesTma ? (const void *)mixed_kernel<8, kMixTilesTma>
+                                    : (const void *)mixed_kernel<8, kMixTiles>;
+    dyn = q.path == kMixTilesTma ? 2ull * p.s * kSlotBytes + 128 : 0;
   }
-  // one instantiation per path, so that each gets its own register allocation
-  const void *kern = p.s > 8                  ? (const void *)mixed_kernel<kMaxStages, kMixTiles>
-                     : q.path == kMixTilesTma ? (const void *)mixed_kernel<8, kMixTilesTma>
-                                              : (const void *)mixed_kernel<8, kMixTiles>;
-  const size_t dyn = q.path == kMixTilesTma ? 2ull * p.s * kSlotBytes + 128 : 0;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
   if (e != cudaSuccess) return e;
   int occ = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kMixThreads, dyn);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, dyn);
   if (e != cudaSuccess) return e;
   if (occ < 1) return cudaErrorInvalidConfiguration;
   int grid = occ * num_sms;
-  const int useful = (p.npairs + kMixThreads - 1) / kMixThreads;
   if (grid > useful) grid = useful > 0 ? useful : 1;
   q.nblocks = grid + (p.extra_arrivals > 0 ? p.extra_arrivals : 0);
   void *args[] = {&q};
   *grid_out = grid;
-  return cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(kMixThreads), args, dyn, stream);
+  return cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(threads), args, dyn, stream);
 }
 
 }  // namespace rkcu

@@ -28,14 +28,19 @@ struct MixedParams {
   CUtensorMap tm[kMixTmaStages];
 };
 
-// How the FP32 stages load their 8 x 32 tiles (with a one-point halo in
-// shared memory): TMA boxes, double-buffered, or plain loads.
-constexpr int kMixTilesTma = 1, kMixTiles = 2;
+// How the FP32 stages run: all stages of a step per 32 x 32 tile in shared
+// memory (kMixFused: F0 and y32 with a halo of s-1 points through TMA, even N
+// and s <= 8), or one stage at a time over 8 x 32 tiles with a one-point halo,
+// their inputs staged by TMA boxes (kMixTilesTma) or plain loads (kMixTiles).
+constexpr int kMixTilesTma = 1, kMixTiles = 2, kMixFused = 3;
 
-// Launches the persistent mixed kernel with the given kMix* path (kMixTilesTma
-// falls back to kMixTiles where TMA boxes do not fit: odd N or more than
-// kMixTmaStages stages).
+// Launches the persistent mixed kernel with the given kMix* path (kMixFused
+// and kMixTilesTma fall back to kMixTiles where TMA boxes do not fit: odd N or
+// more than kMixTmaStages stages).
 cudaError_t launch_mixed(const MixedParams &p, int path, int num_sms, cudaStream_t stream,
                          int *grid_out);
+// Whether kMixFused runs for an N x N grid and s stages (even N, 2 <= s <= 8,
+// TMA available); it needs only the f0 and y32 vectors, not dF_1 .. dF_{s-2}.
+bool mixed_fused_available(int N, int s);
 
 }  // namespace rkcu

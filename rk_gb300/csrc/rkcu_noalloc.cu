@@ -39,7 +39,8 @@ std::mutex g_setup_mutex;
 
 }  // namespace
 
-// 8 MiB + 8.25 KiB per device: all scratch of rkcu_solve_noalloc.
+// All scratch of rkcu_solve_noalloc, per device: 256 B of step-control state,
+// 8 KiB of progress words and 16 vectors of 32768 pairs (8 MiB).
 static __device__ __align__(256) double2 g_noalloc_scratch[kStatePairs + kFlagPairs + kVectors * kPairs];
 
 namespace {
@@ -55,18 +56,16 @@ int scratch_for_current_device(double2 **out) {
   if (!g_scratch_addr[dev]) {
     double2 *p = nullptr;
     e = cudaGetSymbolAddress(reinterpret_cast<void **>(&p), g_noalloc_scratch);
-    if (e != cudaSuccess || !p) return RKCU_ERR_CUDA;
+    if (e != cudaSuccess) return rkcu::record_cuda_error(e, "cudaGetSymbolAddress of the scratch array");
+    if (!p) return RKCU_ERR_CUDA;
     g_scratch_addr[dev] = p;
   }
   *out = g_scratch_addr[dev];
   return RKCU_OK;
 }
 
-int fail_cuda(cudaError_t e, const char *what) {
-  (void)e;
-  (void)what;
-  return RKCU_ERR_CUDA;
-}
+// A failed CUDA call: its text goes where rkcu_last_cuda_error() reads it.
+int fail_cuda(cudaError_t e, const char *what) { return rkcu::record_cuda_error(e, what); }
 
 }  // namespace
 
@@ -159,14 +158,14 @@ extern "C" int rkcu_solve_noalloc(const rkcu_problem *prob, const char *method, 
     if (hs.done) break;
     p.budget = 1 << 20;
     int grid = 0;
-    if ((e = rkcu::launch_plain(p, precision == RKCU_FP64_EXACT ? rkcu::kArithExactSoftMul : rkcu::kArithFused, 0,
-                                   num_sms, st, &grid)) !=
-        cudaSuccess)
+    // the arithmetic rkcu_advance uses for the same precision (same bits either way)
+    const int mode = precision == RKCU_FP64_EXACT ? rkcu::kArithExactSoftMul : rkcu::kArithFusedSoftMul;
+    if ((e = rkcu::launch_plain(p, mode, 0, num_sms, st, &grid)) != cudaSuccess)
       return fail_cuda(e, "step-loop launch");
     if ((e = cudaMemcpyAsync(&hs, dstate, sizeof(hs), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
       return fail_cuda(e, "state download");
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail_cuda(e, "synchronize");
-    if (hs.error) return RKCU_ERR_TIMEOUT;
+    if (hs.error) return rkcu::record_wait_timeout(hs.error_site);
     if (hs.pending) {
       // the step-size update the device left to the C library's pow (tools.h:221-233)
       const double f =

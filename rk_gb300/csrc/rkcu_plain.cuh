@@ -66,6 +66,12 @@ cudaError_t launch_plain(const PlainParams &p, int mode, int blocks_per_sm, int 
 cudaError_t launch_eval_rhs(int problem, const Bruss &bruss, const LvBanded &lvb, int npairs,
                             const double2 *y, double2 *f, cudaStream_t stream);
 
+// Host side: record the text rkcu_last_cuda_error() returns for a failed CUDA
+// call (returns RKCU_ERR_NOMEM or RKCU_ERR_CUDA) or for a device wait that ran
+// out at `site` (returns RKCU_ERR_TIMEOUT).
+int record_cuda_error(cudaError_t e, const char *what);
+int record_wait_timeout(int site);
+
 // Step-size updates on the device (count values), for tests of the controller.
 cudaError_t launch_step_sizes(const double *h, const double *err, int count, double tol, int ord,
                               double *out, cudaStream_t stream);

@@ -9,7 +9,7 @@ import pytest
 
 from conftest import REPO, load_golden
 
-REFERENCE = "/root/reference"
+REFERENCE = os.environ.get("RK_REFERENCE", "/root/reference")
 LIBDIR = os.path.join(REPO, "rk_gb300", "_lib")
 
 

@@ -173,9 +173,10 @@ def test_wait_timeout_is_reported_and_recoverable():
 
 @pytest.mark.parametrize("cfg", [dict(schedule=1), dict(schedule=3),
                                  dict(variant=rk.VARIANT_LOWSTORAGE), dict(precision="mixed"),
+                                 dict(precision="mixed", schedule=2),
                                  dict(precision="mixed", schedule=1)],
-                         ids=["grid-barrier", "flow-tiles", "low-storage", "mixed-tma",
-                              "mixed-plain-loads"])
+                         ids=["grid-barrier", "flow-tiles", "low-storage", "mixed-fused",
+                              "mixed-tma-tiles", "mixed-plain-loads"])
 def test_wait_timeout_in_every_persistent_kernel(cfg):
     """Each persistent kernel's bounded waits end with RKCU_ERR_TIMEOUT when CTAs
     that never exist are awaited; the next solve on the same solver then equals

@@ -50,8 +50,9 @@ def test_serving_admits_by_footprint_and_matches_solo_results():
         y_solo, st_solo = one["results"][0]
         np.testing.assert_array_equal(y_mix, y_solo)
         assert (st_mix["steps_acc"], st_mix["steps_rej"]) == (st_solo["steps_acc"], st_solo["steps_rej"])
-        # and within the requested tolerance of the plain exact path
+        # and equal to the plain exact path (the reference's arithmetic) bit for bit
         p, y0, t0, te, tol = make_request_problem(reqs[i])
         with rk.Solver(p, method="DOPRI54", precision="exact") as s:
-            ref, _ = s.solve(t0, te, y0, tol)
-        assert float(np.max(np.abs(y_mix - ref)) / np.max(np.abs(ref))) <= tol
+            ref, rst = s.solve(t0, te, y0, tol)
+        np.testing.assert_array_equal(y_mix, ref)
+        assert (st_mix["steps_acc"], st_mix["steps_rej"]) == (rst["steps_acc"], rst["steps_rej"])
