@@ -95,6 +95,38 @@ def build_dropin():
     return out
 
 
+# The same drop-in linked with the reference's own main.c, tools.c, methods.c,
+# threads.c and problem module (rk_gb300/dropin/Makefile.cuda), when a copy of
+# the reference sources is at hand (RK_REFERENCE, or the staged copy in
+# baseline/_ref), with the configurations of two golden fixtures; and the
+# reference's sequential D binaries of the same configurations, so that both
+# rows can be read by the reference's log2tab side by side.
+REF_DROPIN = {
+    "bruss2d-mix": ["BRUSS_GRID_SIZE=250", "BRUSS_ALPHA=2E-3", "METHOD=DOPRI54", "TOL=1E-6",
+                    "T_END=0.5", "STEP_LIMIT=0"],
+    "lv": ["LV_COUNT=1000", "METHOD=DOPRI54", "TOL=1E-6", "T_END=10.0", "STEP_LIMIT=0"],
+}
+REF_DROPIN_DIR = os.path.join(LIBDIR, "ref")
+
+
+def build_dropin_reference():
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import stage_reference
+    root = stage_reference.source_root()
+    if not root:
+        return []
+    out = []
+    for problem, defs in REF_DROPIN.items():
+        _run(["make", "-s", "-f", os.path.join(PKG, "dropin", "Makefile.cuda"), "cuda",
+              f"REF={root}", f"BINDIR={REF_DROPIN_DIR}", f"CUDA_PROBLEMS={problem}",
+              "DEFINES=" + " ".join(defs)])
+        out.append(os.path.join(REF_DROPIN_DIR, f"cuda_{problem}_D"))
+        d = dict(x.split("=") for x in defs)
+        d["PROBLEM"] = problem
+        out.append(stage_reference.build_solver("seq/D", d, name=f"seq_{problem}_D_golden"))
+    return out
+
+
 def build_all(verbose=False):
     lib = build_cuda(verbose)
     orc = build_oracle()

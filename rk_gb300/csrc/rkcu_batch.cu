@@ -120,7 +120,8 @@ __global__ void __launch_bounds__(kT, batch_threads_per_sm<kExact>() / kT) batch
   const int gstride = gridDim.x * kT;
   bool ok = true;
 
-  for (int it = 0; it < P.budget; ++it) {
+  const int budget = *(volatile int *)P.budget;
+  for (int it = 0; it < budget; ++it) {
     if (threadIdx.x == 0) {
       s_nch = *(volatile int *)P.nchunks;
       s_clen = *(volatile int *)P.chunk_len;

@@ -58,7 +58,8 @@ struct BatchParams {
   int *rebuild;        // set when an instance finished during a sweep
   int *done_list;      // slots that finished, in order
   int *done_count;
-  int budget;          // sweeps per launch (a sweep = one attempted step of every active instance)
+  int *budget;         // sweeps per launch (device, so that one captured graph serves every
+                       // count; a sweep = one attempted step of every active instance)
   int nblocks;
   unsigned long long timeout_ns;
   DevState *st;        // barrier words and error flag

@@ -51,7 +51,8 @@ struct rkcu_batch {
   InstCoef *d_coef = nullptr;
   int2 *d_chunks = nullptr;
   size_t chunk_cap = 0;
-  int *d_ints = nullptr;  // [0] nslots, [1] nchunks, [2] rebuild, [3] done_count, [4] chunk length
+  int *d_ints = nullptr;  // [0] nslots, [1] nchunks, [2] rebuild, [3] done_count, [4] chunk
+                          // length, [5] sweeps of the next launch
   int *d_done = nullptr;
   DevState *d_st = nullptr;
   rkcu::PowBox *h_box = nullptr;  // mapped, pinned host memory: one mailbox per slot
@@ -68,7 +69,7 @@ struct rkcu_batch {
   int grid = 0;
   // graph
   cudaGraphExec_t graph_exec = nullptr;
-  int graph_budget = 0;
+  int budget = 0;  // sweeps of the launch being set up (the source of the copy to d_ints[5])
   bool use_graph = true;
   long long launches = 0;
   char err[256] = "";
@@ -118,7 +119,7 @@ void arena_free(rkcu_batch *b, size_t off, size_t size) {
   }
 }
 
-BatchParams make_params(rkcu_batch *b, int budget) {
+BatchParams make_params(rkcu_batch *b) {
   BatchParams p;
   std::memset(&p, 0, sizeof(p));
   p.s = b->s;
@@ -143,7 +144,7 @@ BatchParams make_params(rkcu_batch *b, int budget) {
   p.done_list = b->d_done;
   p.chunks = b->d_chunks;
   p.chunk_pairs = b->chunk_pairs;
-  p.budget = budget;
+  p.budget = b->d_ints + 5;
   p.timeout_ns = (unsigned long long)(b->opt.wait_timeout_s * 1e9);
   p.st = b->d_st;
   p.pow_box = b->d_box;
@@ -183,18 +184,19 @@ int wait_serving(rkcu_batch *b) {
 void drop_graph(rkcu_batch *b) {
   if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
   b->graph_exec = nullptr;
-  b->graph_budget = 0;
 }
 
 // One launch of `budget` sweeps: the chunk-list rebuild then the persistent
-// kernel, replayed from a captured CUDA graph when the shape is unchanged.
+// kernel, replayed from a captured CUDA graph when the shape is unchanged (the
+// sweep count is a device word written before each replay).
 int launch(rkcu_batch *b, int budget);
 int launch(rkcu_batch *b, int budget) {
   const bool exact = b->opt.precision != RKCU_FP64_FMA;
+  b->budget = budget;
+  BCK(cudaMemcpyAsync(b->d_ints + 5, &b->budget, sizeof(int), cudaMemcpyHostToDevice, b->stream));
   if (b->use_graph) {
-    if (!b->graph_exec || b->graph_budget != budget) {
-      drop_graph(b);
-      BatchParams p = make_params(b, budget);
+    if (!b->graph_exec) {
+      BatchParams p = make_params(b);
       p.nblocks = rkcu::batch_grid(exact, b->threads, b->blocks_per_sm, b->num_sms);
       cudaGraph_t g = nullptr;
       BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
@@ -216,12 +218,11 @@ int launch(rkcu_batch *b, int budget) {
         b->use_graph = false;
         return launch(b, budget);
       }
-      b->graph_budget = budget;
       b->grid = grid;
     }
     BCK(cudaGraphLaunch(b->graph_exec, b->stream));
   } else {
-    BatchParams p = make_params(b, budget);
+    BatchParams p = make_params(b);
     p.nblocks = rkcu::batch_grid(exact, b->threads, b->blocks_per_sm, b->num_sms);
     BCK(rkcu::launch_batch_rebuild(p, b->stream));
     int grid = 0;
@@ -327,8 +328,8 @@ int rkcu_batch_create(rkcu_batch **out, long long arena_bytes, int max_instances
   b->chunk_cap = b->arena_bytes / (sizeof(double2) * 128) + (size_t)max_instances + 1;
   if ((e = cudaMalloc(&b->d_chunks, sizeof(int2) * b->chunk_cap)) != cudaSuccess)
     return bail(fail(b, e, "chunks"));
-  if ((e = cudaMalloc(&b->d_ints, 5 * sizeof(int))) != cudaSuccess) return bail(fail(b, e, "ints"));
-  if ((e = cudaMemset(b->d_ints, 0, 5 * sizeof(int))) != cudaSuccess) return bail(fail(b, e, "ints"));
+  if ((e = cudaMalloc(&b->d_ints, 6 * sizeof(int))) != cudaSuccess) return bail(fail(b, e, "ints"));
+  if ((e = cudaMemset(b->d_ints, 0, 6 * sizeof(int))) != cudaSuccess) return bail(fail(b, e, "ints"));
   if ((e = cudaMalloc(&b->d_done, sizeof(int) * max_instances)) != cudaSuccess)
     return bail(fail(b, e, "done list"));
   if ((e = cudaMalloc(&b->d_st, sizeof(DevState))) != cudaSuccess) return bail(fail(b, e, "state"));

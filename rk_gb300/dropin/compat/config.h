@@ -31,5 +31,15 @@
 #ifndef METHOD
 #define METHOD DOPRI54
 #endif
+/* lock type and padding of the reference's pthreads runtime (config.h:100-121);
+   only printed here, as the reference's main does, for log2tab */
+#define MUTEX 0
+#define SPINLOCK 1
+#ifndef LOCKTYPE
+#define LOCKTYPE MUTEX
+#endif
+#ifndef PAD_SIZE
+#define PAD_SIZE 128
+#endif
 
 #endif

@@ -170,6 +170,12 @@ int main(void)
   printf("Initial value: y0[0] = %e, ..., y0[%d] = %e; min = %e, max = %e\n", y0[0],
          ode_size - 1, y0[ode_size - 1], lo, hi);
   printf("Tolerance: %.2e\n", tol);
+#if LOCKTYPE == SPINLOCK
+  printf("Lock type: spin\n");
+#else
+  printf("Lock type: mutex\n");
+#endif
+  printf("Pad size: %d\n", PAD_SIZE);
 
   timer_start(&timer);
   solver(T_START, T_END, y0, y, tol);

@@ -7,6 +7,10 @@ batch, whose persistent kernel advances every admitted solve by a few sweeps
 per launch.  Requests that arrive while others are on the GPU are admitted
 between launches as slots and memory free up, so their work overlaps on the
 device; finished solves are copied out and their space reused at once.
+The launches are time slices: the sweep count of the next launch is chosen
+from the measured time per sweep so that a launch lasts about `slice_s`,
+which bounds how long an arriving request waits for admission while the
+sweeps stay long enough to keep the GPU busy.
 Latency of a request = completion time - arrival time.
 """
 import time
@@ -26,12 +30,30 @@ def make_request_problem(req):
 
 
 class ServingLoop:
-    def __init__(self, arena_bytes, max_instances=4096, sweeps_per_launch=32, precision="exact",
-                 method="DOPRI54", device=0, stream=None):
+    """sweeps_per_launch > 0 fixes the sweeps per launch; 0 chooses them per
+    launch as a time slice of about slice_s (a power of two, 1 .. max_sweeps)."""
+
+    def __init__(self, arena_bytes, max_instances=4096, sweeps_per_launch=0, precision="exact",
+                 method="DOPRI54", device=0, stream=None, slice_s=0.004, max_sweeps=64):
         self.batch = rk.Batch(arena_bytes, max_instances, method=method, precision=precision,
                               device=device, stream=stream)
-        self.sweeps = sweeps_per_launch
+        self.fixed = sweeps_per_launch
+        self.sweeps = sweeps_per_launch if sweeps_per_launch > 0 else 4
+        self.slice_s = slice_s
+        self.max_sweeps = max_sweeps
+        self.sweep_s = None               # running estimate of one sweep's time
         self.stages = rk.builtin_method(method)["s"]
+
+    def _run_slice(self):
+        """One launch; updates the per-sweep time estimate and the next sweep count."""
+        t = time.perf_counter()
+        active = self.batch.run(self.sweeps)
+        dt = (time.perf_counter() - t) / self.sweeps
+        if not self.fixed:
+            self.sweep_s = dt if self.sweep_s is None else 0.7 * self.sweep_s + 0.3 * dt
+            want = max(1.0, self.slice_s / max(self.sweep_s, 1e-7))
+            self.sweeps = int(min(self.max_sweeps, 2 ** int(np.floor(np.log2(want)))))
+        return active
 
     def close(self):
         self.batch.close()
@@ -81,7 +103,7 @@ class ServingLoop:
             if not tuned and active >= tune_after:
                 self.batch.tune(1)
                 tuned = True
-            active = self.batch.run(self.sweeps)
+            active = self._run_slice()
             for slot in self.batch.finished():
                 y, st, i = self.batch.take(slot)
                 finish[i] = time.perf_counter() - t_start

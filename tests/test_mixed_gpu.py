@@ -59,7 +59,7 @@ N4000 = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "n400
 def n4000_fixture():
     """The FP64 final state of the N=4000 solve at its stored sample indices
     (tests/golden/make_n4000_fixture.py) and the fixture's record."""
-    sys.path.insert(0, os.path.dirname(N4000 + ".json"))
+    sys.path.insert(0, os.path.dirname(os.path.dirname(N4000)))  # tests/golden
     with open(N4000 + ".json") as f:
         rec = json.load(f)
     from make_n4000_fixture import sample_indices

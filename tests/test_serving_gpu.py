@@ -28,7 +28,7 @@ def test_serving_admits_by_footprint_and_matches_solo_results():
     reqs = _requests()
     fps = [rk.footprint(make_request_problem(r)[0], 7) for r in reqs]
     arena = int(sum(sorted(fps)[-2:]))          # room for about two of the largest at once
-    loop = ServingLoop(arena, max_instances=64, sweeps_per_launch=8)
+    loop = ServingLoop(arena, max_instances=64)      # launches as time slices
     try:
         out = loop.serve(reqs, keep_results=True)
     finally:
