@@ -58,10 +58,14 @@ def stage():
     return STAGED
 
 
-def build_solver(variant, defines, name=None, root=None):
+def build_solver(variant, defines, name=None, root=None, contract=True):
     """Compile bin/<name> from the reference's main.c, tools.c, methods.c, threads.c,
     problems/bruss2d-mix.c (or lv.c: defines containing "PROBLEM=lv") and
-    src/impl/<variant>.c.  Returns the executable's path, or None without sources."""
+    src/impl/<variant>.c.  contract=False adds -ffp-contract=off: the
+    reference's flags leave multiply-add contraction to the compiler, which
+    fuses on aarch64 and not on x86-64, so only without contraction are its
+    results the same on both (and equal to the golden fixtures).  Returns the
+    executable's path, or None without sources."""
     root = root or source_root()
     if not root:
         return None
@@ -74,6 +78,7 @@ def build_solver(variant, defines, name=None, root=None):
     src += [os.path.join(root, "src", "problems", problem + ".c"),
             os.path.join(root, "src", "impl", variant + ".c")]
     cmd = ["gcc", "-I" + os.path.join(root, "include"), *REF_CFLAGS,
+           *([] if contract else ["-ffp-contract=off"]),
            *[f"-D{k}={v}" for k, v in defines.items()], "-o", exe, *src, *REF_LDFLAGS]
     subprocess.run(cmd, check=True, capture_output=True)
     return exe

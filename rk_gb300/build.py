@@ -119,11 +119,13 @@ def build_dropin_reference():
     for problem, defs in REF_DROPIN.items():
         _run(["make", "-s", "-f", os.path.join(PKG, "dropin", "Makefile.cuda"), "cuda",
               f"REF={root}", f"BINDIR={REF_DROPIN_DIR}", f"CUDA_PROBLEMS={problem}",
+              "CUDA_EXTRA_CFLAGS=-ffp-contract=off",
               "DEFINES=" + " ".join(defs)])
         out.append(os.path.join(REF_DROPIN_DIR, f"cuda_{problem}_D"))
         d = dict(x.split("=") for x in defs)
         d["PROBLEM"] = problem
-        out.append(stage_reference.build_solver("seq/D", d, name=f"seq_{problem}_D_golden"))
+        out.append(stage_reference.build_solver("seq/D", d, name=f"seq_{problem}_D_golden",
+                                                contract=False))
     return out
 
 

@@ -381,8 +381,8 @@ int rkcu_begin(rkcu_solver *s, double t0, double te, const double *y0, int y0_on
   if (s->prob.problem == RKCU_PROBLEM_RHS && !s->rhs) return RKCU_ERR_STATE;
   RKCU_CK(cudaSetDevice(s->opt.device));
   if (s->opt.precision == RKCU_MIXED) {
-    // f0, y32 and, unless all FP32 stages run per tile in shared memory, dF[1..s-2]
-    const int mneed = mixed_path(s) == rkcu::kMixFused ? 2 : s->s;
+    // f0, y32, f0lo and, unless all FP32 stages run per tile in shared memory, dF[1..s-2]
+    const int mneed = mixed_path(s) == rkcu::kMixFused ? 3 : s->s + 1;
     if (s->mstage_vectors < mneed) {
       if (s->mstage) {
         RKCU_CK(cudaStreamSynchronize(s->stream));
@@ -545,9 +545,10 @@ int rkcu_advance(rkcu_solver *s, int max_steps) {
     const size_t np = s->npairs;
     m.f0 = s->mstage;
     m.y32 = s->mstage + np;
+    m.f0lo = s->mstage + 2 * np;
     // the dF vectors exist unless the FP32 stages run per tile in shared memory
-    if (s->mstage_vectors >= s->s)
-      for (int j = 1; j <= s->s - 2; ++j) m.dF[j] = s->mstage + (size_t)(1 + j) * np;
+    if (s->mstage_vectors >= s->s + 1)
+      for (int j = 1; j <= s->s - 2; ++j) m.dF[j] = s->mstage + (size_t)(2 + j) * np;
     m.st = s->st;
     m.bruss.N = s->prob.grid_n;
     m.bruss.coef = bruss_coef(&s->prob);

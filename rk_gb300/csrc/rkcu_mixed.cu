@@ -8,21 +8,22 @@
 //                                       on the integer pipe, the rest in FP32
 //                                       pairs (about 2^-46 relative), FP64 only
 //                                       where a value leaves those ranges
-//   y1 = y + (h * sum b) * F0           FP64 sums of y and the double-float
-//                                       product, the large part of the update
 //   stage i >= 1:  delta_i = h c_i F0 + sum_{1<=j<i} h a_ij dF_j                (FP32)
 //                  dF_i = f(y + delta_i) - F0 = alpha (N-1)^2 lap(delta_i)
 //                         + [u^2 v](y + delta) - [u^2 v](y) -/+ 4.4 du / 3.4 du  (FP32)
 //     (the Laplacian is linear, and the cubic term is expanded exactly, so the
 //      large diffusion coefficient never multiplies FP32 rounding of y itself)
 //   dY = sum_{j>=1} h b_j dF_j          FP32, Kahan-compensated, in order of j
-//   e  = sum_{j>=1} h (b_j - b^_j) dF_j FP32 (the F0 terms cancel: sum(b - b^) = 0)
-//   y_new = y1 + dY                     FP64
+//   inc = (h * sum b) * F0 + dY         double-float
+//   y_new = (y + inc.hi) + inc.lo       two FP64 sums
+//   e  = h sum(b - b^) F0 + sum_{j>=1} h (b_j - b^_j) dF_j
+//                                       double-float (the F0 term is nearly
+//                                       zero: sum(b - b^) = 0)
 //   err max = max |e| / max(|y_new|, |y_old|): per thread in FP32, reduced in FP64
 // c_i is taken as the row sum of A (sum_j a_ij), so sum_j h a_ij F0 = h c_i F0.
-// FP64 instructions per component-step: 3 (the sums of the update; the
+// FP64 instructions per component-step: 2 (the sums of the update; the
 // conversions between float and double are built from bit fields) instead of
-// 85-128 for the FP64 forms.
+// 54-73 on the FP64 pipe for the FP64 forms.
 //
 // Memory: this form is bound by HBM traffic, not arithmetic, so it stores each
 // stage's dF_i once and gathers delta_i from dF_1 .. dF_{i-1} at the five
@@ -131,19 +132,20 @@ __device__ __forceinline__ dfl::df df_term(float c_hi, float c_lo, float x) {
 }
 
 // The step's update at one grid point from its stage increments d[1..s-2]
-// and dlast (dF_1 .. dF_{s-1}) and F0 (f):
-//   dY = sum_j h b_j dF_j     FP32, Kahan-compensated, in stage order
-//   y_new = y1 + dY           FP64 (y1 = y + h sum(b) F0 from stage 0)
+// and dlast (dF_1 .. dF_{s-1}), F0 as a double-float pair (f, flo) and y:
+//   dY  = sum_j h b_j dF_j          FP32, Kahan-compensated, in stage order
+//   inc = h sum(b) F0 + dY          double-float (about 2^-44 relative)
+//   y_new = (y + inc.hi) + inc.lo   two FP64 sums, the form's only FP64 work
 //   e = h sum(b - b^) F0 + sum_j h (b_j - b^_j) dF_j
-//                             double-float: every product to about 2^-47, the
-//                             sum to about 2^-44 relative, in stage order
+//                                   double-float: every product to about 2^-47,
+//                                   the sum to about 2^-44 relative, in stage order
 // and the error ratios |e| / max(|y_new|, |y|) of the pair's two components
 // (FP32 from the estimate's leading part; a zero divisor gives 3e38, so the
 // step is rejected, as the reference's 1.7e308 of include/tools.h:284 would).
 template <int kMaxS>
 __device__ __forceinline__ double2 mix_update(const float2 (&d)[kMaxS], float2 dlast, int s, float2 f,
-                                              float2 y32, double2 y1, const MixCoef &c, float *rx,
-                                              float *ry) {
+                                              float2 flo, float2 y32, double2 y, dfl::df hbd,
+                                              const MixCoef &c, float *rx, float *ry) {
   float2 sum = make_float2(0.f, 0.f), cmp = make_float2(0.f, 0.f);
   dfl::df ex = df_term(c.hbhs_hi, c.hbhs_lo, f.x), ey = df_term(c.hbhs_hi, c.hbhs_lo, f.y);
 #pragma unroll
@@ -159,8 +161,10 @@ __device__ __forceinline__ double2 mix_update(const float2 (&d)[kMaxS], float2 d
     ex = dfl::df_add(ex, df_term(c.hbh_hi[jj], c.hbh_lo[jj], dj.x));
     ey = dfl::df_add(ey, df_term(c.hbh_hi[jj], c.hbh_lo[jj], dj.y));
   }
-  const double2 yn = make_double2(__dadd_rn(y1.x, dfl::dbl_of(sum.x - cmp.x)),
-                                  __dadd_rn(y1.y, dfl::dbl_of(sum.y - cmp.y)));
+  const dfl::df ix = dfl::df_add(dfl::df_mul(hbd, {f.x, flo.x}), dfl::fast_two_sum(sum.x, -cmp.x));
+  const dfl::df iy = dfl::df_add(dfl::df_mul(hbd, {f.y, flo.y}), dfl::fast_two_sum(sum.y, -cmp.y));
+  const double2 yn = make_double2(__dadd_rn(__dadd_rn(y.x, dfl::dbl_of(ix.hi)), dfl::dbl_of(ix.lo)),
+                                  __dadd_rn(__dadd_rn(y.y, dfl::dbl_of(iy.hi)), dfl::dbl_of(iy.lo)));
   const float dnx = fmaxf(fabsf(trunc_to_float(yn.x)), fabsf(y32.x));
   const float dny = fmaxf(fabsf(trunc_to_float(yn.y)), fabsf(y32.y));
   const float erx = ex.hi + ex.lo, ery = ey.hi + ey.lo;
@@ -176,7 +180,7 @@ __device__ __forceinline__ double2 mix_update(const float2 (&d)[kMaxS], float2 d
 // (with a halo of s-1 points) are read from memory, one TMA box each,
 // double-buffered, and only y_new is written.
 constexpr int kFT = 32;
-constexpr int kFusedThreads = 512;
+constexpr int kFusedThreads = 1024;
 constexpr int mix_threads(int path) { return path == kMixFused ? kFusedThreads : kMixThreads; }
 
 template <int kS>
@@ -206,12 +210,12 @@ __device__ __forceinline__ void static_for(F &&f) {
 // Out of line, so that its FP64 instructions are not if-converted into the
 // double-float loop.
 static __device__ __noinline__ void stage0_point_fp64(const Bruss &br, const double2 *__restrict__ ycur, int p,
-                                                      double hbs, double2 *__restrict__ ynew,
-                                                      float2 *__restrict__ f0) {
+                                                      float2 *__restrict__ f0, float2 *__restrict__ f0lo) {
   const double2 F = br.eval<kArithFusedSoftMul>(ycur, p);
-  const double2 Y = ycur[p];
-  ynew[p] = make_double2(fma(hbs, F.x, Y.x), fma(hbs, F.y, Y.y));
-  f0[p] = make_float2(softfp::to_float(F.x), softfp::to_float(F.y));
+  const float hx = softfp::to_float(F.x), hy = softfp::to_float(F.y);
+  f0[p] = make_float2(hx, hy);
+  f0lo[p] = make_float2(softfp::to_float(F.x - static_cast<double>(hx)),
+                        softfp::to_float(F.y - static_cast<double>(hy)));
 }
 
 // kMaxS: an upper bound of the stage count (8 or 13), so that the per-stage
@@ -237,7 +241,6 @@ __global__ void __launch_bounds__(mix_threads(kPath), kPath == kMixFused ? 1 : (
   __shared__ int s_jl[kMaxStages][kMaxStages];
   __shared__ float s_ja[kMaxStages][kMaxStages];
   __shared__ int s_nj[kMaxStages];
-  __shared__ double s_hbsum;
   __shared__ float s_hbs_hi, s_hbs_lo;  // h sum(b) as a double-float pair
   __shared__ float2 s_delta[kTileR + 2][kTileC + 2];  // delta_i on a tile and its halo
 
@@ -294,9 +297,9 @@ __global__ void __launch_bounds__(mix_threads(kPath), kPath == kMixFused ? 1 : (
       s_coef.hbh_lo[j] = static_cast<float>(hbh - static_cast<double>(s_coef.hbh_hi[j]));
     }
     if (threadIdx.x == 0) {
-      s_hbsum = h * P.bsum;
-      s_hbs_hi = static_cast<float>(s_hbsum);
-      s_hbs_lo = static_cast<float>(s_hbsum - static_cast<double>(s_hbs_hi));
+      const double hbs = h * P.bsum;
+      s_hbs_hi = static_cast<float>(hbs);
+      s_hbs_lo = static_cast<float>(hbs - static_cast<double>(s_hbs_hi));
       const double hbhs = h * P.bhsum;
       s_coef.hbhs_hi = static_cast<float>(hbhs);
       s_coef.hbhs_lo = static_cast<float>(hbhs - static_cast<double>(s_coef.hbhs_hi));
@@ -306,10 +309,10 @@ __global__ void __launch_bounds__(mix_threads(kPath), kPath == kMixFused ? 1 : (
     double2 *__restrict__ ynew = P.y[s_cur ^ 1];
 
     // stage 0: F0 = f(y) in double-float (fixed-point Laplacian, FP32 pairs),
-    // y1 = y + h sum(b) F0 in FP64, F0 and y rounded to FP32; a point whose
-    // values fall outside the double-float ranges takes the FP64 evaluation
+    // stored as its leading (f0) and trailing (f0lo) floats, and y rounded to
+    // FP32; a point whose values fall outside the double-float ranges takes
+    // the FP64 evaluation
     {
-      const dfl::df hbd = {s_hbs_hi, s_hbs_lo};
       const int N = br.N;
       // grid point (k, j) of pair p, advanced by the grid stride without a division
       const int dk = gstride / N, dj = gstride - dk * N;
@@ -328,12 +331,10 @@ __global__ void __launch_bounds__(mix_threads(kPath), kPath == kMixFused ? 1 : (
         const double2 e = row[j == N - 1 ? j - 1 : j + 1];
         dfl::df fu, fv;
         if (dfl::bruss_rhs_df(c, up, dn, w, e, coef_df, &fu, &fv)) {
-          const dfl::df qu = dfl::df_mul(hbd, fu), qv = dfl::df_mul(hbd, fv);
-          ynew[p] = make_double2(__dadd_rn(__dadd_rn(c.x, dfl::dbl_of(qu.hi)), dfl::dbl_of(qu.lo)),
-                                 __dadd_rn(__dadd_rn(c.y, dfl::dbl_of(qv.hi)), dfl::dbl_of(qv.lo)));
           P.f0[p] = make_float2(fu.hi, fv.hi);
+          P.f0lo[p] = make_float2(fu.lo, fv.lo);
         } else {
-          stage0_point_fp64(br, ycur, p, s_hbsum, ynew, P.f0);
+          stage0_point_fp64(br, ycur, p, P.f0, P.f0lo);
         }
         P.y32[p] = make_float2(trunc_to_float(c.x), trunc_to_float(c.y));
       }
@@ -343,6 +344,7 @@ __global__ void __launch_bounds__(mix_threads(kPath), kPath == kMixFused ? 1 : (
 
     float emax = 0.0f;
     const int N = br.N;
+    const dfl::df hbd = {s_hbs_hi, s_hbs_lo};  // h sum(b)
     if constexpr (kPath == kMixFused) {
       // All FP32 stages per tile (FusedGeom): F0 and y32 frames through TMA,
       // double-buffered; delta_i and dF_i in shared-memory frames.
@@ -382,65 +384,92 @@ __global__ void __launch_bounds__(mix_threads(kPath), kPath == kMixFused ? 1 : (
         }
         const int k0 = (t / tiles_x) * kFT, j0 = (t % tiles_x) * kFT;
         const float2 *const ff0 = frame(2 * b), *const fy32 = frame(2 * b + 1);
-        static_for<1, kMaxS>([&](auto ic) {
-          constexpr int i = decltype(ic)::value;
-          // delta_i on the tile and a halo of s-i points (frame rows/columns
-          // HY-dd.., HX-dd..); points outside the grid are never read
-          constexpr int dd = kMaxS - i, RD = kFT + 2 * dd;
-          const int nj = s_nj[i];
-          const float hci = hc[i];
-          for (int idx = threadIdx.x; got && idx < RD * RD; idx += kFusedThreads) {
-            const int r = idx / RD, c = idx - (idx / RD) * RD;
-            const int k = k0 - dd + r, j = j0 - dd + c;
-            if (static_cast<unsigned>(k) >= static_cast<unsigned>(N) ||
-                static_cast<unsigned>(j) >= static_cast<unsigned>(N))
-              continue;
-            const int e = (G::HY - dd + r) * G::FC + (G::HX - dd + c);
-            float2 acc = make_float2(0.0f, 0.0f);
+        // A tile whose regions lie inside the grid away from its edges (all but
+        // the outermost ring of tiles) needs no bounds checks and no boundary
+        // stencils: its loops are compiled without them.
+        const bool interior = k0 >= kMaxS - 1 && j0 >= kMaxS - 1 && k0 + kFT + kMaxS - 1 <= N &&
+                              j0 + kFT + kMaxS - 1 <= N;
+        auto stages = [&](auto interior_c) {
+          constexpr bool kIn = decltype(interior_c)::value;
+          static_for<1, kMaxS>([&](auto ic) {
+            constexpr int i = decltype(ic)::value;
+            // delta_i on the tile and a halo of s-i points (frame rows/columns
+            // HY-dd.., HX-dd..); points outside the grid are never read
+            constexpr int dd = kMaxS - i, RD = kFT + 2 * dd;
+            constexpr int kJ = i > 1 ? i - 1 : 1;
+            constexpr int eb_d = (G::HY - dd) * G::FC + (G::HX - dd);
+            const int nj = s_nj[i];
+            const float hci = hc[i];
+            const float2 *jf[kJ];
+            float ja[kJ];
 #pragma unroll
-            for (int kk = 0; kk < (i > 1 ? i - 1 : 1); ++kk) {
-              if (kk < nj) {
-                const float a = s_ja[i][kk];
-                const float2 d = frame(4 + s_jl[i][kk])[e];
-                acc.x = fmaf(a, d.x, acc.x);
-                acc.y = fmaf(a, d.y, acc.y);
+            for (int kk = 0; kk < kJ; ++kk) {
+              jf[kk] = frame(4 + (kk < nj ? s_jl[i][kk] : 1));
+              ja[kk] = kk < nj ? s_ja[i][kk] : 0.0f;
+            }
+            for (int idx = threadIdx.x; got && idx < RD * RD; idx += kFusedThreads) {
+              const int r = idx / RD, c = idx - r * RD;
+              if constexpr (!kIn) {
+                const int k = k0 - dd + r, j = j0 - dd + c;
+                if (static_cast<unsigned>(k) >= static_cast<unsigned>(N) ||
+                    static_cast<unsigned>(j) >= static_cast<unsigned>(N))
+                  continue;
+              }
+              const int e = eb_d + r * G::FC + c;
+              float2 acc = make_float2(0.0f, 0.0f);
+#pragma unroll
+              for (int kk = 0; kk < kJ; ++kk) {
+                if (kk < nj) {
+                  const float2 d = jf[kk][e];
+                  acc.x = fmaf(ja[kk], d.x, acc.x);
+                  acc.y = fmaf(ja[kk], d.y, acc.y);
+                }
+              }
+              const float2 f = ff0[e];
+              fd[e] = make_float2(fmaf(hci, f.x, acc.x), fmaf(hci, f.y, acc.y));
+            }
+            __syncthreads();
+            // dF_i on the tile and a halo of s-1-i points
+            constexpr int dq = kMaxS - 1 - i, RQ = kFT + 2 * dq;
+            constexpr int eb_q = (G::HY - dq) * G::FC + (G::HX - dq);
+            for (int idx = threadIdx.x; got && idx < RQ * RQ; idx += kFusedThreads) {
+              const int r = idx / RQ, c = idx - r * RQ;
+              const int k = k0 - dq + r, j = j0 - dq + c;
+              const int e = eb_q + r * G::FC + c;
+              int eu = e - G::FC, en = e + G::FC, jcase = 0;
+              if constexpr (!kIn) {
+                if (static_cast<unsigned>(k) >= static_cast<unsigned>(N) ||
+                    static_cast<unsigned>(j) >= static_cast<unsigned>(N))
+                  continue;
+                // a boundary row or column uses its inner neighbour twice
+                if (k == 0) eu = en;
+                if (k == N - 1) en = eu;
+                jcase = j == 0 ? 1 : (j == N - 1 ? 2 : 0);
+              }
+              const float2 dF = delta_rhs(fd[e], fd[eu], fd[en], fd[e - 1], fd[e + 1], jcase, fy32[e], coef);
+              if constexpr (i < kMaxS - 1) {
+                frame(4 + i)[e] = dF;
+              } else {
+                // the last stage: the update and the error ratio at the tile's point
+                float2 dall[kMaxS];
+                dall[0] = make_float2(0.f, 0.f);
+#pragma unroll
+                for (int jj = 1; jj < kMaxS - 1; ++jj) dall[jj] = frame(4 + jj)[e];
+                const size_t p = static_cast<size_t>(k) * N + j;
+                float rx, ry;
+                ynew[p] = mix_update<kMaxS>(dall, dF, kMaxS, ff0[e], P.f0lo[p], fy32[e], ycur[p], hbd, s_coef,
+                                            &rx, &ry);
+                emax = fmaxf(emax, rx);
+                if (2 * p + 1 < static_cast<size_t>(P.n)) emax = fmaxf(emax, ry);
               }
             }
-            const float2 f = ff0[e];
-            fd[e] = make_float2(fmaf(hci, f.x, acc.x), fmaf(hci, f.y, acc.y));
-          }
-          __syncthreads();
-          // dF_i on the tile and a halo of s-1-i points
-          constexpr int dq = kMaxS - 1 - i, RQ = kFT + 2 * dq;
-          for (int idx = threadIdx.x; got && idx < RQ * RQ; idx += kFusedThreads) {
-            const int r = idx / RQ, c = idx - (idx / RQ) * RQ;
-            const int k = k0 - dq + r, j = j0 - dq + c;
-            if (static_cast<unsigned>(k) >= static_cast<unsigned>(N) ||
-                static_cast<unsigned>(j) >= static_cast<unsigned>(N))
-              continue;
-            const int e = (G::HY - dq + r) * G::FC + (G::HX - dq + c);
-            // a boundary row or column uses its inner neighbour twice
-            const int eu = k == 0 ? e + G::FC : e - G::FC;
-            const int en = k == N - 1 ? e - G::FC : e + G::FC;
-            const int jcase = j == 0 ? 1 : (j == N - 1 ? 2 : 0);
-            const float2 dF = delta_rhs(fd[e], fd[eu], fd[en], fd[e - 1], fd[e + 1], jcase, fy32[e], coef);
-            if constexpr (i < kMaxS - 1) {
-              frame(4 + i)[e] = dF;
-            } else {
-              // the last stage: the update and the error ratio at the tile's point
-              float2 dall[kMaxS];
-              dall[0] = make_float2(0.f, 0.f);
-#pragma unroll
-              for (int jj = 1; jj < kMaxS - 1; ++jj) dall[jj] = frame(4 + jj)[e];
-              const size_t p = static_cast<size_t>(k) * N + j;
-              float rx, ry;
-              ynew[p] = mix_update<kMaxS>(dall, dF, kMaxS, ff0[e], fy32[e], ynew[p], s_coef, &rx, &ry);
-              emax = fmaxf(emax, rx);
-              if (2 * p + 1 < static_cast<size_t>(P.n)) emax = fmaxf(emax, ry);
-            }
-          }
-          if constexpr (i < kMaxS - 1) __syncthreads();
-        });
+            if constexpr (i < kMaxS - 1) __syncthreads();
+          });
+        };
+        if (interior)
+          stages(std::true_type{});
+        else
+          stages(std::false_type{});
       }
       if (__syncthreads_or(bad)) ok = false;
       if (!ok) break;
@@ -457,7 +486,7 @@ __global__ void __launch_bounds__(mix_threads(kPath), kPath == kMixFused ? 1 : (
       // dF_i (and, in the last stage, dY, e and y_new) at grid point p from
       // delta_i on the tile (s_delta), y32, and the point's own dF_j / f0
       auto finish_point_at = [&](int p, int k, int j, float2 c, float2 up, float2 dn, float2 w,
-                                 float2 e, float2 y32, auto &&own_dF, auto &&own_f0, auto &&own_y1) {
+                                 float2 e, float2 y32, auto &&own_dF, auto &&own_f0) {
         const int jcase = j == 0 ? 1 : (j == N - 1 ? 2 : 0);
         const float2 dF = delta_rhs(c, up, dn, w, e, jcase, y32, coef);
         if (!last) {
@@ -471,16 +500,16 @@ __global__ void __launch_bounds__(mix_threads(kPath), kPath == kMixFused ? 1 : (
         for (int jj = 1; jj < kMaxS; ++jj)
           if (jj < s - 1) dall[jj] = own_dF(jj);
         float rx, ry;
-        ynew[p] = mix_update<kMaxS>(dall, dF, s, own_f0(), y32, own_y1(), s_coef, &rx, &ry);
+        ynew[p] = mix_update<kMaxS>(dall, dF, s, own_f0(), P.f0lo[p], y32, ycur[p], hbd, s_coef, &rx, &ry);
         emax = fmaxf(emax, rx);
         if (2 * p + 1 < P.n) emax = fmaxf(emax, ry);
       };
       auto finish_point = [&](int tr_, int tc_, int k, int j, float2 y32, auto &&own_dF,
-                              auto &&own_f0, auto &&own_y1) {
+                              auto &&own_f0) {
         finish_point_at(k * N + j, k, j, s_delta[tr_ + 1][tc_ + 1],
                         s_delta[k == 0 ? tr_ + 2 : tr_][tc_ + 1],
                         s_delta[k == N - 1 ? tr_ : tr_ + 2][tc_ + 1], s_delta[tr_ + 1][tc_],
-                        s_delta[tr_ + 1][tc_ + 2], y32, own_dF, own_f0, own_y1);
+                        s_delta[tr_ + 1][tc_ + 2], y32, own_dF, own_f0);
       };
 
       if constexpr (kPath == kMixTilesTma) {
@@ -558,7 +587,7 @@ __global__ void __launch_bounds__(mix_threads(kPath), kPath == kMixFused ? 1 : (
             const int eo = (tr + 1) * kBoxPairs + tc + 2;  // the point itself in a box
             finish_point(tr, tc, k, j, slot(b, 1)[eo],
                          [&](int jj) { return slot(b, 1 + jj)[eo]; },
-                         [&]() { return bf0[eo]; }, [&]() { return ynew[k * N + j]; });
+                         [&]() { return bf0[eo]; });
           }
         }
         if (__syncthreads_or(bad)) ok = false;
@@ -581,7 +610,7 @@ __global__ void __launch_bounds__(mix_threads(kPath), kPath == kMixFused ? 1 : (
           if (k >= N || j >= N) continue;
           const int p = k * N + j;
           finish_point(tr, tc, k, j, P.y32[p], [&](int jj) { return P.dF[jj][p]; },
-                       [&]() { return P.f0[p]; }, [&]() { return ynew[p]; });
+                       [&]() { return P.f0[p]; });
         }
       }
       if (!last) {

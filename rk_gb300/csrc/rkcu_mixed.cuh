@@ -21,6 +21,7 @@ struct MixedParams {
   unsigned char nzA[kMaxStages * kMaxStages];
   double2 *y[2];
   float2 *f0, *y32;
+  float2 *f0lo;            // F0 = f0 + f0lo, a double-float pair per component
   float2 *dF[kMaxStages];  // dF[1 .. s-2]: the stages' right-hand-side increments
   DevState *st;
   Bruss bruss;
