@@ -191,8 +191,10 @@ struct FusedGeom {
   static constexpr int FR = kFT + 2 * HY, FC = kFT + 2 * HX;  // frame rows, columns
   static constexpr int kFrame = FR * FC;                  // points (float2) per frame
   static constexpr unsigned kFrameBytes = (kFrame * 8u + 127u) / 128u * 128u;
-  // F0 and y32 twice (double buffer), delta, dF_1 .. dF_{s-2}
-  static constexpr int kFrames = 5 + (kS > 2 ? kS - 2 : 0);
+  // F0 and y32 twice (double buffer), delta twice (this stage's and the
+  // next one's), dF_1 .. dF_{s-2}
+  static constexpr int kFrames = 6 + (kS > 2 ? kS - 2 : 0);
+  static constexpr int kDelta = 4, kDF = 5;  // frame of delta_i: kDelta + (i & 1); of dF_j: kDF + j
   static constexpr size_t kSmem = static_cast<size_t>(kFrames) * kFrameBytes + 128;
   static_assert(2 * FC <= 256 && FR <= 256, "TMA box dimensions are at most 256 elements");
 };
@@ -352,7 +354,6 @@ __global__ void __launch_bounds__(mix_threads(kPath), kPath == kMixFused ? 1 : (
       auto frame = [&](int f) { return reinterpret_cast<float2 *>(s_box + static_cast<size_t>(f) * G::kFrameBytes); };
       const int tiles_x = (N + kFT - 1) / kFT;
       const int ntiles = tiles_x * tiles_x;
-      float2 *const fd = frame(4);
       auto issue = [&](int t, int b) {
         const int k0 = (t / tiles_x) * kFT, j0 = (t % tiles_x) * kFT;
         mbar_arrive_expect_tx(&s_mbar[b], 2u * G::kFrame * 8u);
@@ -391,47 +392,30 @@ __global__ void __launch_bounds__(mix_threads(kPath), kPath == kMixFused ? 1 : (
                               j0 + kFT + kMaxS - 1 <= N;
         auto stages = [&](auto interior_c) {
           constexpr bool kIn = decltype(interior_c)::value;
+          // One pass per stage i over the tile and a halo of s-1-i points:
+          // dF_i from delta_i's stencil, and at the same point delta_{i+1} =
+          // h c_{i+1} F0 + sum_{j<=i} h a_{i+1,j} dF_j (the region the next
+          // stage's stencil reads); delta_1 = h c_1 F0 comes from F0 itself.
           static_for<1, kMaxS>([&](auto ic) {
             constexpr int i = decltype(ic)::value;
-            // delta_i on the tile and a halo of s-i points (frame rows/columns
-            // HY-dd.., HX-dd..); points outside the grid are never read
-            constexpr int dd = kMaxS - i, RD = kFT + 2 * dd;
-            constexpr int kJ = i > 1 ? i - 1 : 1;
-            constexpr int eb_d = (G::HY - dd) * G::FC + (G::HX - dd);
-            const int nj = s_nj[i];
-            const float hci = hc[i];
-            const float2 *jf[kJ];
-            float ja[kJ];
-#pragma unroll
-            for (int kk = 0; kk < kJ; ++kk) {
-              jf[kk] = frame(4 + (kk < nj ? s_jl[i][kk] : 1));
-              ja[kk] = kk < nj ? s_ja[i][kk] : 0.0f;
-            }
-            for (int idx = threadIdx.x; got && idx < RD * RD; idx += kFusedThreads) {
-              const int r = idx / RD, c = idx - r * RD;
-              if constexpr (!kIn) {
-                const int k = k0 - dd + r, j = j0 - dd + c;
-                if (static_cast<unsigned>(k) >= static_cast<unsigned>(N) ||
-                    static_cast<unsigned>(j) >= static_cast<unsigned>(N))
-                  continue;
-              }
-              const int e = eb_d + r * G::FC + c;
-              float2 acc = make_float2(0.0f, 0.0f);
-#pragma unroll
-              for (int kk = 0; kk < kJ; ++kk) {
-                if (kk < nj) {
-                  const float2 d = jf[kk][e];
-                  acc.x = fmaf(ja[kk], d.x, acc.x);
-                  acc.y = fmaf(ja[kk], d.y, acc.y);
-                }
-              }
-              const float2 f = ff0[e];
-              fd[e] = make_float2(fmaf(hci, f.x, acc.x), fmaf(hci, f.y, acc.y));
-            }
-            __syncthreads();
-            // dF_i on the tile and a halo of s-1-i points
+            constexpr bool kLast = i == kMaxS - 1;
             constexpr int dq = kMaxS - 1 - i, RQ = kFT + 2 * dq;
             constexpr int eb_q = (G::HY - dq) * G::FC + (G::HX - dq);
+            constexpr int kJ = i;  // delta_{i+1} sums over j = 1 .. i
+            const float2 *const fdi = i == 1 ? ff0 : frame(G::kDelta + (i & 1));
+            const float sdi = i == 1 ? hc[1] : 1.0f;  // delta_1 = h c_1 F0
+            float2 *const fdn = frame(G::kDelta + ((i + 1) & 1));
+            const int nj = kLast ? 0 : s_nj[i + 1];
+            const float hcn = kLast ? 0.0f : hc[i + 1];
+            const float2 *jf[kJ];
+            float ja[kJ];
+            int jl[kJ];
+#pragma unroll
+            for (int kk = 0; kk < kJ; ++kk) {
+              jl[kk] = kk < nj ? s_jl[i + 1][kk] : 0;
+              ja[kk] = kk < nj ? s_ja[i + 1][kk] : 0.0f;
+              jf[kk] = frame(G::kDF + (jl[kk] >= 1 && jl[kk] < i ? jl[kk] : 1));
+            }
             for (int idx = threadIdx.x; got && idx < RQ * RQ; idx += kFusedThreads) {
               const int r = idx / RQ, c = idx - r * RQ;
               const int k = k0 - dq + r, j = j0 - dq + c;
@@ -446,15 +430,30 @@ __global__ void __launch_bounds__(mix_threads(kPath), kPath == kMixFused ? 1 : (
                 if (k == N - 1) en = eu;
                 jcase = j == 0 ? 1 : (j == N - 1 ? 2 : 0);
               }
-              const float2 dF = delta_rhs(fd[e], fd[eu], fd[en], fd[e - 1], fd[e + 1], jcase, fy32[e], coef);
-              if constexpr (i < kMaxS - 1) {
-                frame(4 + i)[e] = dF;
+              auto dl = [&](int x) {
+                const float2 v = fdi[x];
+                return i == 1 ? make_float2(fmaf(sdi, v.x, 0.0f), fmaf(sdi, v.y, 0.0f)) : v;
+              };
+              const float2 dF = delta_rhs(dl(e), dl(eu), dl(en), dl(e - 1), dl(e + 1), jcase, fy32[e], coef);
+              if constexpr (!kLast) {
+                if constexpr (i <= kMaxS - 2) frame(G::kDF + i)[e] = dF;
+                float2 acc = make_float2(0.0f, 0.0f);
+#pragma unroll
+                for (int kk = 0; kk < kJ; ++kk) {
+                  if (kk < nj) {
+                    const float2 d = jl[kk] == i ? dF : jf[kk][e];
+                    acc.x = fmaf(ja[kk], d.x, acc.x);
+                    acc.y = fmaf(ja[kk], d.y, acc.y);
+                  }
+                }
+                const float2 f = ff0[e];
+                fdn[e] = make_float2(fmaf(hcn, f.x, acc.x), fmaf(hcn, f.y, acc.y));
               } else {
                 // the last stage: the update and the error ratio at the tile's point
                 float2 dall[kMaxS];
                 dall[0] = make_float2(0.f, 0.f);
 #pragma unroll
-                for (int jj = 1; jj < kMaxS - 1; ++jj) dall[jj] = frame(4 + jj)[e];
+                for (int jj = 1; jj < kMaxS - 1; ++jj) dall[jj] = frame(G::kDF + jj)[e];
                 const size_t p = static_cast<size_t>(k) * N + j;
                 float rx, ry;
                 ynew[p] = mix_update<kMaxS>(dall, dF, kMaxS, ff0[e], P.f0lo[p], fy32[e], ycur[p], hbd, s_coef,
@@ -463,7 +462,7 @@ __global__ void __launch_bounds__(mix_threads(kPath), kPath == kMixFused ? 1 : (
                 if (2 * p + 1 < static_cast<size_t>(P.n)) emax = fmaxf(emax, ry);
               }
             }
-            if constexpr (i < kMaxS - 1) __syncthreads();
+            if constexpr (!kLast) __syncthreads();
           });
         };
         if (interior)
