@@ -57,7 +57,7 @@ FP64_PER_SM_CLK = 2.0
 MEASURED_TRAFFIC = {
     ("d", "exact", "DOPRI54"): (584.0, "one-pass ncu capture of the 61 timed launches of this benchmark's default command"),
     ("d", "fma", "DOPRI54"): (573.0, "ncu --set full of a 3-step launch at N=2000"),
-    ("d", "mixed", "DOPRI54"): (164.0, "ncu --set full of a 3-step launch at N=2000, scaled by n"),
+    ("d", "mixed", "DOPRI54"): (46.9, "ncu --set full of a 3-step launch at N=2000 (fused FP32 stages), scaled by n"),
 }
 
 KERNEL_NAME = {"d": "plain_kernel (persistent, all stages of K steps)",
@@ -504,7 +504,7 @@ def form_mixed(rk, device, peak, peak_kind):
         "unit": "steps/s", "steps": steps, "accepted": st["steps_acc"], "rejected": st["steps_rej"],
         "ms_per_step": ms / steps, "dtype": "f32 stages / f64 state", "gpu_launches": launches,
         "config": {"workload": f"bruss2d-mix N={rec['grid_n']} n={n} DOPRI54 tol=1e-6 t=[0,0.5], "
-                               "the whole solve", "l2": "2 x 256 MB FP64 state + 7 x 128 MB FP32 "
+                               "the whole solve", "l2": "2 x 256 MB FP64 state + 3 x 128 MB FP32 "
                                "vectors > 129 MB L2, no flush"},
         "e2e": {"value": steps / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": 8.0 * n / steps,
                 "d2h_bytes_per_step": 8.0 * n / steps},
@@ -516,8 +516,11 @@ def form_mixed(rk, device, peak, peak_kind):
                               rec["mixed"]["rel_max_norm_full"]},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
+                     "traffic": tr[0] * n * steps / max(1, launches) if tr else None,
                      "traffic_bytes_per_component_step": tr[0] if tr else None,
-                     "traffic_source": tr[1] if tr else None},
+                     "traffic_source": tr[1] if tr else None,
+                     "dram_frac": tr[0] * n * steps / (ms * 1e-3) / 1e9 / peak if tr else None,
+                     "kernel": "mixed_kernel (persistent; stage 0, then all FP32 stages per tile)"},
         "clocks": clk,
     }
 
