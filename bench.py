@@ -446,7 +446,7 @@ def run_ours(args):
         line["mixed"] = form_mixed(rk, local, peak, peak_kind)
         line["batched"] = form_batched(rk, args.batched_sample, not args.no_cpu_baseline)
         cap = line["batched"]["component_steps_per_s"]
-        line["served"] = [form_served(rk, args.served_requests, load, cap) for load in (0.5, 0.9)]
+        line["served"] = [form_served(rk, args.served_requests, load, cap) for load in (0.5, 0.9, 1.5)]
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -721,19 +721,24 @@ def run_batched(args):
                      for k, d in enumerate(sample))
     value = len(sample) / (ms * 1e-3)
 
-    # plain form on a sub-sample (one solve after another), same instance distribution
-    sub = list(range(0, len(sample), max(1, len(sample) // args.plain_sample)))[: args.plain_sample]
+    # plain form, one solve after another: on every instance (--plain-sample 0), or on
+    # a sub-sample with its time scaled by component-steps
+    if args.plain_sample <= 0:
+        sub = list(range(len(sample)))
+    else:
+        sub = list(range(0, len(sample), max(1, len(sample) // args.plain_sample)))[: args.plain_sample]
     t = time.perf_counter()
-    plain_cs = 0
+    same = 0
     for k in sub:
         with rk.Solver(probs[k], method="DOPRI54", precision=args.precision) as s:
             y, st = s.solve(0.0, 0.5, y0s[k], sample[k]["tol"])
-        plain_cs += 2 * sample[k]["grid_n"] ** 2 * (st["steps_acc"] + st["steps_rej"])
+        same += int(np.array_equal(y, results[k][0]))
     plain_s = time.perf_counter() - t
     sub_cs = sum(2 * sample[k]["grid_n"] ** 2 * (results[k][1]["steps_acc"] + results[k][1]["steps_rej"])
                  for k in sub)
-    # the plain form's solves/s on the whole sample, scaled by component-steps
     plain_value = len(sample) / (plain_s * comp_steps / max(1, sub_cs))
+    plain_note = ("every instance, one solve after another" if len(sub) == len(sample) else
+                  f"{len(sub)} instances solved one after another, scaled by work")
 
     line = {
         "metric": "batched BRUSS2D-MIX solves/s (4096-instance distribution)", "value": value,
@@ -745,8 +750,9 @@ def run_batched(args):
                    "tuned_ns_per_pair_step": tuned_ns,
                    "component_steps": comp_steps},
         "component_steps_per_s": comp_steps / (ms * 1e-3),
-        "plain_form": {"value": plain_value, "unit": "solves/s",
-                       "sample": f"{len(sub)} instances solved one after another, scaled by work"},
+        "plain_form": {"value": plain_value, "unit": "solves/s", "sample": plain_note,
+                       "results_bit_identical_to_batch": same},
+        "host_pow_steps": sum(results[k][1]["host_pow_steps"] for k in results),
         "e2e": {"value": len(sample) / e2e_s, "unit": "solves/s",
                 "h2d_bytes_per_step": sum(8 * p.n for p in probs) / max(1, sweeps),
                 "d2h_bytes_per_step": sum(8 * p.n for p in probs) / max(1, sweeps)},

@@ -88,7 +88,9 @@ typedef struct
   int schedule;         /* plain form, stage synchronisation: 0 = automatic (neighbour
                            flags), 1 = grid barrier after every stage, 2 = neighbour
                            progress flags, 3 = dataflow over (stage, tile) in wavefront
-                           order; mixed form: 0 = automatic (3 where it runs: even
+                           order, 4 = neighbour flags with each stage input's grid
+                           rows staged in shared memory by bulk copies (BRUSS2D-MIX,
+                           N <= 3600; others use 2); mixed form: 0 = automatic (3 where it runs: even
                            N, at most 8 stages; else 2), 1 = one stage at a time
                            over tiles with plain loads, 2 = the same with TMA-staged
                            tiles, 3 = all FP32 stages of a step per tile in shared

@@ -263,7 +263,7 @@ int rkcu_create(rkcu_solver **out, const rkcu_problem *prob, const rkcu_options 
   if (o.step_limit < 0) return RKCU_ERR_INVALID;
   if (!(o.wait_timeout_s > 0.0)) o.wait_timeout_s = 10.0;
   if (!(o.h_init >= 0.0)) return RKCU_ERR_INVALID;
-  if (o.schedule < 0 || o.schedule > 3 || o.flow_skew < 0) return RKCU_ERR_INVALID;
+  if (o.schedule < 0 || o.schedule > 4 || o.flow_skew < 0) return RKCU_ERR_INVALID;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= o.device || o.device < 0)
     return RKCU_ERR_NO_DEVICE;
@@ -594,6 +594,10 @@ int rkcu_advance(rkcu_solver *s, int max_steps) {
   p.schedule = s->opt.schedule == 1   ? rkcu::kScheduleGrid
                : s->opt.schedule == 3 ? rkcu::kScheduleFlow
                                       : rkcu::kScheduleNeighbour;
+  // the row ring stages BRUSS2D-MIX grid rows in shared memory (N up to kRowRingMaxN)
+  if (s->opt.schedule == 4 && s->prob.problem == RKCU_PROBLEM_BRUSS2D_MIX &&
+      s->prob.grid_n <= rkcu::kRowRingMaxN)
+    p.schedule = rkcu::kScheduleRowRing;
   flow_geometry(s, &p.flow_tile, &p.flow_ntiles, &p.flow_dep);
   p.flow_skew = s->opt.flow_skew;  // 0: chosen at launch from the grid size
   // the flow schedule's tile counters hold step * s + stage within a launch

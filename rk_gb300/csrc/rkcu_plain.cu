@@ -27,11 +27,16 @@
 #include <type_traits>
 
 #include "rkcu_plain.cuh"
+#include "rkcu_tma.cuh"
 #include "rkcu.h"
 
 namespace rkcu {
 
 constexpr int kThreads = 256;
+// Row-ring schedule (kScheduleRowRing): one CTA of kRingThreads per SM, the
+// stage input's grid rows staged in a ring of kRingSlots rows of shared memory.
+constexpr int kRingThreads = 1024;
+constexpr int kRingSlots = 4;
 // Chunks of blockDim pairs by which the L2 bulk prefetch runs ahead (0: off).
 constexpr int kL2Ahead = 0;
 
@@ -83,17 +88,19 @@ constexpr int plain_rhs_mode() {
   return kExact == kArithExactSoftMul ? kArithExact : kExact;
 }
 
-template <class Prob, int kExact>
-__global__ void __launch_bounds__(kThreads, plain_min_blocks<Prob, kExact>()) plain_kernel(const __grid_constant__ PlainParams P) {
+template <class Prob, int kExact, bool kRing>
+__global__ void __launch_bounds__(kRing ? kRingThreads : kThreads, kRing ? 1 : plain_min_blocks<Prob, kExact>())
+    plain_kernel(const __grid_constant__ PlainParams P) {
   using M = Arith<kExact>;
   constexpr int kRhs = plain_rhs_mode<kExact>();
+  constexpr int kT = kRing ? kRingThreads : kThreads;
   __shared__ double hA[kMaxStages * kMaxStages];
   __shared__ double hb[kMaxStages], hbh[kMaxStages];
   __shared__ double s_t, s_h;
   __shared__ int s_acc, s_rej, s_cur, s_done, s_pending;
   __shared__ unsigned long long s_step;
   __shared__ double s_pend_err, s_pend_h;
-  __shared__ double s_wmax[kThreads / 32];
+  __shared__ double s_wmax[kT / 32];
   __shared__ unsigned int s_tk[2];
 
   const Prob &prob = problem_of<Prob>(P);
@@ -112,6 +119,20 @@ __global__ void __launch_bounds__(kThreads, plain_min_blocks<Prob, kExact>()) pl
     s_pending = st->pending;
     s_pend_err = st->pend_err;
     s_pend_h = st->pend_h;
+  }
+  // row ring: kRingSlots rows of pairs in dynamic shared memory, one mbarrier
+  // per slot; rpar holds the parity each slot's next completion will have
+  extern __shared__ __align__(128) unsigned char s_ring_raw[];
+  __shared__ __align__(8) uint64_t s_rbar[kRingSlots];
+  unsigned rpar = 0, rpend = 0;  // rpend: slots with a copy issued and not yet waited for
+  auto ring_row = [&](int q) {
+    return reinterpret_cast<double2 *>(s_ring_raw) + static_cast<size_t>(q) * prob.row_pairs();
+  };
+  if constexpr (kRing) {
+    if (threadIdx.x == 0) {
+      for (int q = 0; q < kRingSlots; ++q) mbar_init(&s_rbar[q], 1);
+      mbar_fence_init();
+    }
   }
   __syncthreads();
 
@@ -154,10 +175,8 @@ __global__ void __launch_bounds__(kThreads, plain_min_blocks<Prob, kExact>()) pl
     double2 *__restrict__ ytr =
         (P.trace_y && kstep < P.trace_cap) ? P.trace_y + static_cast<size_t>(kstep) * P.npairs : nullptr;
 
-    // first stage at pair p (block-inline.h:253-272)
-    auto stage_first = [&](int p, int k, int j) {
-      const double2 F = prob.template eval_kj<kRhs>(ycur, p, k, j);
-      const double2 Y = ycur[p];
+    // first stage at pair p (block-inline.h:253-272), from F = f(y) and y at p
+    auto stage_first_f = [&](int p, const double2 F, const double2 Y) {
       for (int l = 1; l < s; ++l) {
         double2 wv = Y;
         if (P.nzA[l * kMaxStages]) {
@@ -170,9 +189,11 @@ __global__ void __launch_bounds__(kThreads, plain_min_blocks<Prob, kExact>()) pl
       P.dy[p] = make_double2(M::mul(hb[0], F.x), M::mul(hb[0], F.y));
       P.err[p] = make_double2(M::mul(hbh[0], F.x), M::mul(hbh[0], F.y));
     };
-    // intermediate stage i at pair p (block-inline.h:276-294)
-    auto stage_mid = [&](int i, int p, int k, int j) {
-      const double2 F = prob.template eval_kj<kRhs>(P.w[i], p, k, j);
+    auto stage_first = [&](int p, int k, int j) {
+      stage_first_f(p, prob.template eval_kj<kRhs>(ycur, p, k, j), ycur[p]);
+    };
+    // intermediate stage i at pair p (block-inline.h:276-294), from F = f(w_i) at p
+    auto stage_mid_f = [&](int i, int p, const double2 F) {
       for (int l = i + 1; l < s; ++l) {
         if (!P.nzA[l * kMaxStages + i]) continue;
         const double a = hA[l * kMaxStages + i];
@@ -196,11 +217,14 @@ __global__ void __launch_bounds__(kThreads, plain_min_blocks<Prob, kExact>()) pl
         P.err[p] = e;
       }
     };
-    // last stage at pair p (block-inline.h:298-320) and its error terms (tools.h:280-288)
+    auto stage_mid = [&](int i, int p, int k, int j) {
+      stage_mid_f(i, p, prob.template eval_kj<kRhs>(P.w[i], p, k, j));
+    };
+    // last stage at pair p (block-inline.h:298-320) and its error terms
+    // (tools.h:280-288), from F = f(w_{s-1}) at p
     ErrMax em;
-    auto stage_last = [&](int p, int k, int j) {
+    auto stage_last_f = [&](int p, const double2 F) {
       const int i = s - 1;
-      const double2 F = prob.template eval_kj<kRhs>(P.w[i], p, k, j);
       double2 d = P.dy[p];
       double2 e = P.err[p];
       if (P.nzb[i]) {
@@ -217,6 +241,9 @@ __global__ void __launch_bounds__(kThreads, plain_min_blocks<Prob, kExact>()) pl
       if (ytr) ytr[p] = yn;
       em.add(e.x, yn.x, Y.x);
       if (2 * p + 1 < P.n) em.add(e.y, yn.y, Y.y);
+    };
+    auto stage_last = [&](int p, int k, int j) {
+      stage_last_f(p, prob.template eval_kj<kRhs>(P.w[s - 1], p, k, j));
     };
 
     // Software prefetch (to L1) of the next pair's stage vectors, in the fused
@@ -333,6 +360,77 @@ __global__ void __launch_bounds__(kThreads, plain_min_blocks<Prob, kExact>()) pl
         slot ^= 1;
       }
       if (!ok) break;
+    } else if constexpr (kRing) {
+      // Row ring (BRUSS2D-MIX): for each stage, the stage input's grid rows that
+      // this CTA's pairs and their stencils touch arrive by 1-D bulk copies
+      // (TMA) into a ring of kRingSlots rows of shared memory, one row ahead of
+      // the row being computed; the stencil reads shared memory, the other
+      // vectors are read and written in place.
+      auto ring_stage = [&](const double2 *src, auto &&body) {
+        const int N = rowN;
+        if (lo >= hi) return true;
+        const int r0 = lo / N, r1 = (hi - 1) / N;
+        const unsigned row_bytes = static_cast<unsigned>(N) * 16u;
+        auto issue = [&](int r) {
+          if (r < 0 || r >= N || r > r1 + 1 || r < r0 - 1) return;
+          const int q = r % kRingSlots;
+          mbar_arrive_expect_tx(&s_rbar[q], row_bytes);
+          bulk_load(ring_row(q), src + static_cast<size_t>(r) * N, row_bytes, &s_rbar[q]);
+          rpend |= 1u << q;
+        };
+        auto wait_row = [&](int r) {
+          if (r < 0 || r >= N || r > r1 + 1) return true;
+          const int q = r % kRingSlots;
+          const bool got = mbar_wait(&s_rbar[q], (rpar >> q) & 1u, st, P.timeout_ns, 5);
+          if (got) {
+            rpar ^= 1u << q;
+            rpend &= ~(1u << q);
+          }
+          return got;
+        };
+        // rows r0 - 1 .. r0 + kRingSlots - 2 first; then, once row r is done (its
+        // up row's slot is free), row r + kRingSlots - 1
+        if (threadIdx.x == 0)
+          for (int r = r0 - 1; r <= r0 + kRingSlots - 2; ++r) issue(r);
+        bool good = wait_row(r0 - 1) & wait_row(r0);
+        for (int r = r0; r <= r1; ++r) {
+          good = wait_row(r + 1) && good;
+          if (__syncthreads_or(!good)) return false;
+          const double2 *cr = ring_row(r % kRingSlots);
+          const double2 *up = ring_row((r == 0 ? 1 : r - 1) % kRingSlots);
+          const double2 *dn = ring_row((r == N - 1 ? N - 2 : r + 1) % kRingSlots);
+          const int jlo = max(lo, r * N) - r * N, jhi = min(hi, (r + 1) * N) - r * N;
+          for (int j = jlo + threadIdx.x; j < jhi; j += kT) body(r * N + j, r, j, up, cr, dn);
+          __syncthreads();
+          if (threadIdx.x == 0) issue(r + kRingSlots - 1);
+        }
+        return true;
+      };
+      auto ring_eval = [&](const double2 *up, const double2 *cr, const double2 *dn, int j) {
+        return prob.template eval_rows<kRhs>(up, cr, dn, j);
+      };
+      // generic-proxy writes of this stage, read by later bulk copies (this CTA's
+      // and its neighbours'), are ordered before the progress flag
+      ok = ring_stage(ycur, [&](int p, int, int j, const double2 *up, const double2 *cr, const double2 *dn) {
+        stage_first_f(p, ring_eval(up, cr, dn, j), cr[j]);
+      });
+      if (!ok) break;
+      fence_proxy_async_global();
+      if (!(ok = stage_sync(P, c_lo, c_hi, ++progress, 1))) break;
+      for (int i = 1; i < s - 1; ++i) {
+        ok = ring_stage(P.w[i], [&](int p, int, int j, const double2 *up, const double2 *cr, const double2 *dn) {
+          stage_mid_f(i, p, ring_eval(up, cr, dn, j));
+        });
+        if (!ok) break;
+        fence_proxy_async_global();
+        if (!(ok = stage_sync(P, c_lo, c_hi, ++progress, 2))) break;
+      }
+      if (!ok) break;
+      ok = ring_stage(P.w[s - 1], [&](int p, int, int j, const double2 *up, const double2 *cr, const double2 *dn) {
+        stage_last_f(p, ring_eval(up, cr, dn, j));
+      });
+      if (!ok) break;
+      fence_proxy_async_global();  // y_new is the next step's bulk-copied input
     } else {
       for (GridCursor g(p0, rowN); g.p < pend; g.advance(pstep, dk_s, dj_s, rowN)) {
         pf_first(g.p + pstep);
@@ -362,7 +460,7 @@ __global__ void __launch_bounds__(kThreads, plain_min_blocks<Prob, kExact>()) pl
     __syncthreads();
     if (threadIdx.x == 0) {
       double m = s_wmax[0];
-      for (int k = 1; k < kThreads / 32; ++k) m = fmax(m, s_wmax[k]);
+      for (int k = 1; k < kT / 32; ++k) m = fmax(m, s_wmax[k]);
       atomicMax(&st->err_slot[s_step & 1], (unsigned long long)__double_as_longlong(m));
     }
     if (!(ok = grid_barrier(st, P.nblocks, P.timeout_ns, 3))) break;
@@ -417,6 +515,14 @@ __global__ void __launch_bounds__(kThreads, plain_min_blocks<Prob, kExact>()) pl
     if (s_pending) break;  // the host finishes this step's size update
   }
 
+  // after a wait that ran out of time, let the row copies still in flight land
+  // before the CTA leaves (bounded as well)
+  if constexpr (kRing) {
+    if (rpend && threadIdx.x == 0)
+      for (int q = 0; q < kRingSlots; ++q)
+        if ((rpend >> q) & 1u) mbar_wait(&s_rbar[q], (rpar >> q) & 1u, st, P.timeout_ns, 6);
+  }
+
   if (ok && blockIdx.x == 0 && threadIdx.x == 0) {
     st->t = s_t;
     st->h = s_h;
@@ -442,7 +548,32 @@ __global__ void __launch_bounds__(kThreads) eval_rhs_kernel(Prob prob, int npair
 template <class Prob, int kExact>
 static cudaError_t launch_one(const PlainParams &p, int blocks_per_sm, int num_sms,
                               cudaStream_t stream, int *grid_out) {
-  auto kern = plain_kernel<Prob, kExact>;
+  if constexpr (std::is_same<Prob, Bruss>::value) {
+    if (p.schedule == kScheduleRowRing) {
+      // one CTA of kRingThreads per SM with the row ring in dynamic shared memory
+      auto kern = plain_kernel<Prob, kExact, true>;
+      const size_t dyn = static_cast<size_t>(kRingSlots) * p.bruss.N * sizeof(double2);
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+      if (e != cudaSuccess) return e;
+      int occ = 0;
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kRingThreads, dyn);
+      if (e != cudaSuccess) return e;
+      if (occ < 1) return cudaErrorInvalidConfiguration;
+      int grid = occ * num_sms;
+      const int useful = (p.npairs + kRingThreads - 1) / kRingThreads;
+      if (grid > useful) grid = useful > 0 ? useful : 1;
+      if (grid > kMaxPlainGrid) grid = kMaxPlainGrid;
+      PlainParams q = p;
+      q.nblocks = grid + (p.extra_arrivals > 0 ? p.extra_arrivals : 0);
+      void *args[] = {&q};
+      *grid_out = grid;
+      e = cudaMemsetAsync(p.flags, 0, sizeof(unsigned int) * grid, stream);
+      if (e != cudaSuccess) return e;
+      return cudaLaunchCooperativeKernel((const void *)kern, dim3(grid), dim3(kRingThreads), args, dyn,
+                                         stream);
+    }
+  }
+  auto kern = plain_kernel<Prob, kExact, false>;
   int occ = 0;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kThreads, 0);
   if (e != cudaSuccess) return e;

@@ -29,7 +29,8 @@ struct PlainParams {
   DevState *st;
   unsigned int *flags;                // progress words (reset by each launch): kMaxPlainGrid
                                       // CTA words, or the flow schedule's 2 tickets + tiles
-  int schedule;                       // kScheduleGrid, kScheduleNeighbour or kScheduleFlow
+  int schedule;                       // kScheduleGrid, kScheduleNeighbour, kScheduleFlow or
+                                      // kScheduleRowRing
   int flow_tile;                      // flow schedule: pairs per tile
   int flow_ntiles;                    //   tiles per stage
   int flow_dep;                       //   tiles either side a stage's stencil reads
@@ -54,6 +55,11 @@ constexpr int kMaxPlainGrid = 2048;
 constexpr int kScheduleGrid = 1;
 constexpr int kScheduleNeighbour = 2;
 constexpr int kScheduleFlow = 3;
+// Neighbour progress flags between stages, with each stage input's grid rows
+// staged in shared memory by bulk copies (BRUSS2D-MIX; one CTA per SM).
+constexpr int kScheduleRowRing = 4;
+// Largest grid the row ring holds (kRingSlots rows of N pairs in 227 KB).
+constexpr int kRowRingMaxN = 3600;
 // Progress words the flow schedule needs for ntiles tiles.
 inline size_t flow_words(int ntiles) { return 2 + static_cast<size_t>(ntiles); }
 

@@ -70,6 +70,16 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, i
       : "memory");
 }
 
+// 1-D bulk copy of `bytes` (a multiple of 16) from global to shared memory,
+// both addresses 16-byte aligned; completes bytes on the mbarrier.
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
 // order this thread's generic-proxy global writes before later async-proxy
 // (TMA) reads of the same memory
 __device__ __forceinline__ void fence_proxy_async_global() {

@@ -171,11 +171,11 @@ def test_wait_timeout_is_reported_and_recoverable():
     assert st["steps_acc"] + st["steps_rej"] == rec["steps"]
 
 
-@pytest.mark.parametrize("cfg", [dict(schedule=1), dict(schedule=3),
+@pytest.mark.parametrize("cfg", [dict(schedule=1), dict(schedule=3), dict(schedule=4),
                                  dict(variant=rk.VARIANT_LOWSTORAGE), dict(precision="mixed"),
                                  dict(precision="mixed", schedule=2),
                                  dict(precision="mixed", schedule=1)],
-                         ids=["grid-barrier", "flow-tiles", "low-storage", "mixed-fused",
+                         ids=["grid-barrier", "flow-tiles", "row-ring", "low-storage", "mixed-fused",
                               "mixed-tma-tiles", "mixed-plain-loads"])
 def test_wait_timeout_in_every_persistent_kernel(cfg):
     """Each persistent kernel's bounded waits end with RKCU_ERR_TIMEOUT when CTAs

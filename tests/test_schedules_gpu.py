@@ -2,7 +2,9 @@
 
 The plain kernel can close a stage with a grid barrier (schedule 1), with
 neighbour progress flags (2, also the automatic choice 0 that the other tests
-use), or run a dataflow over (stage, tile) tickets in wavefront order (3).  Every schedule applies the same operations in the same
+use), or run a dataflow over (stage, tile) tickets in wavefront order (3), or
+stage each stage input's grid rows in a shared-memory ring by bulk copies (4,
+BRUSS2D-MIX; LV falls back to 2).  Every schedule applies the same operations in the same
 order to every component, so the exact mode must reproduce the reference's
 golden results bit for bit under each, for any tile size and skew.
 """
@@ -39,7 +41,8 @@ def _solve(rec, **kw):
     dict(schedule=3),
     dict(schedule=3, flow_skew=1),
     dict(schedule=3, flow_skew=5, block_rows=2),
-], ids=["grid-barrier", "flow-auto", "flow-k1", "flow-k5-r2"])
+    dict(schedule=4),
+], ids=["grid-barrier", "flow-auto", "flow-k1", "flow-k5-r2", "row-ring"])
 def test_schedule_matches_reference(name, sched):
     rec = load_golden(name)
     y, st = _solve(rec, **sched)
@@ -69,3 +72,24 @@ def test_flow_schedule_fma_and_trace():
         s.set_trace(rec["steps"], with_y=False)
         s.solve(rec["t0"], rec["t_end"], golden_y0(rec), rec["tol"])
         assert [float(v).hex() for v in s.trace()["h"]] == rec["h_trace"]
+
+
+def test_row_ring_fma_trace_and_n2000():
+    """The row ring also serves the FMA mode and the per-step trace, and at the
+    FP64 configuration's size its steps equal the default schedule's bit for bit."""
+    rec = load_golden("bruss_n32_rkf23")
+    a, _ = _solve(rec, precision="fma")
+    b, _ = _solve(rec, precision="fma", schedule=4)
+    np.testing.assert_array_equal(a, b)
+    with rk.Solver(_problem(rec), method=rec["method"], schedule=4) as s:
+        s.set_trace(rec["steps"], with_y=False)
+        s.solve(rec["t0"], rec["t_end"], golden_y0(rec), rec["tol"])
+        assert [float(v).hex() for v in s.trace()["h"]] == rec["h_trace"]
+    prob = rk.bruss2d_mix(2000, 2e-3)
+    y0 = rk.ode_start(prob)
+    out = []
+    for sched in (0, 4):
+        with rk.Solver(prob, method="DOPRI54", precision="exact", schedule=sched, step_limit=40) as s:
+            out.append(s.solve(0.0, 0.5, y0, 1e-6))
+    assert (out[0][1]["steps_acc"], out[0][1]["steps_rej"]) == (out[1][1]["steps_acc"], out[1][1]["steps_rej"])
+    np.testing.assert_array_equal(out[0][0], out[1][0])
