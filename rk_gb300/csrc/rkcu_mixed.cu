@@ -140,9 +140,8 @@ __device__ __forceinline__ dfl::df df_term(float c_hi, float c_lo, float x) {
 //                                   double-float: every product to about 2^-47,
 //                                   the sum to about 2^-44 relative, in stage order
 // and the error ratios |e| / max(|y_new|, |y|) of the pair's two components
-// (FP32 from the estimate's leading part, to 2 ulp; a zero divisor gives 3e38,
-// so the step is rejected, as the reference's 1.7e308 of include/tools.h:284
-// would).
+// (FP32 from the estimate's leading part; a zero divisor gives 3e38, so the
+// step is rejected, as the reference's 1.7e308 of include/tools.h:284 would).
 template <int kMaxS>
 __device__ __forceinline__ double2 mix_update(const float2 (&d)[kMaxS], float2 dlast, int s, float2 f,
                                               float2 flo, float2 y32, double2 y, dfl::df hbd,
@@ -169,10 +168,8 @@ __device__ __forceinline__ double2 mix_update(const float2 (&d)[kMaxS], float2 d
   const float dnx = fmaxf(fabsf(trunc_to_float(yn.x)), fabsf(y32.x));
   const float dny = fmaxf(fabsf(trunc_to_float(yn.y)), fabsf(y32.y));
   const float erx = ex.hi + ex.lo, ery = ey.hi + ey.lo;
-  // the ratio only meets the tolerance in a comparison: the fast division (2 ulp)
-  // is ample; divisors above 2^126 (outside its range) use the rounded one
-  *rx = dnx == 0.0f ? 3.0e38f : dnx < 1e37f ? __fdividef(fabsf(erx), dnx) : fabsf(erx) / dnx;
-  *ry = dny == 0.0f ? 3.0e38f : dny < 1e37f ? __fdividef(fabsf(ery), dny) : fabsf(ery) / dny;
+  *rx = dnx == 0.0f ? 3.0e38f : fabsf(erx) / dnx;
+  *ry = dny == 0.0f ? 3.0e38f : fabsf(ery) / dny;
   return yn;
 }
 
@@ -184,8 +181,6 @@ __device__ __forceinline__ double2 mix_update(const float2 (&d)[kMaxS], float2 d
 // double-buffered, and only y_new is written.
 constexpr int kFT = 32;
 constexpr int kFusedThreads = 1024;
-// Interior tiles evaluate two points per thread and iteration in stages 1 .. s-2.
-constexpr bool kFusedPairs = true;
 constexpr int mix_threads(int path) { return path == kMixFused ? kFusedThreads : kMixThreads; }
 
 template <int kS>
@@ -421,48 +416,6 @@ __global__ void __launch_bounds__(mix_threads(kPath), kPath == kMixFused ? 1 : (
               ja[kk] = kk < nj ? s_ja[i + 1][kk] : 0.0f;
               jf[kk] = frame(G::kDF + (jl[kk] >= 1 && jl[kk] < i ? jl[kk] : 1));
             }
-            if constexpr (kIn && !kLast && kFusedPairs) {
-              // interior tile, not the last stage: two points per thread and
-              // iteration, all loads of both before any store, so that their
-              // shared-memory and arithmetic latencies overlap (the second
-              // point of the last iteration may not exist)
-              auto dl = [&](int x) {
-                const float2 v = fdi[x];
-                return i == 1 ? make_float2(fmaf(sdi, v.x, 0.0f), fmaf(sdi, v.y, 0.0f)) : v;
-              };
-              for (int idx = threadIdx.x; got && idx < RQ * RQ; idx += 2 * kFusedThreads) {
-                const bool two = idx + kFusedThreads < RQ * RQ;
-                const int ib = two ? idx + kFusedThreads : idx;
-                const int ra = idx / RQ, rb = ib / RQ;
-                const int ea = eb_q + ra * G::FC + (idx - ra * RQ);
-                const int eb = eb_q + rb * G::FC + (ib - rb * RQ);
-                const float2 ac = dl(ea), au = dl(ea - G::FC), ad = dl(ea + G::FC), aw = dl(ea - 1),
-                             ae = dl(ea + 1), ay = fy32[ea];
-                const float2 bc = dl(eb), bu = dl(eb - G::FC), bd = dl(eb + G::FC), bw = dl(eb - 1),
-                             be = dl(eb + 1), by = fy32[eb];
-                const float2 dFa = delta_rhs(ac, au, ad, aw, ae, 0, ay, coef);
-                const float2 dFb = delta_rhs(bc, bu, bd, bw, be, 0, by, coef);
-                float2 acca = make_float2(0.0f, 0.0f), accb = make_float2(0.0f, 0.0f);
-#pragma unroll
-                for (int kk = 0; kk < kJ; ++kk) {
-                  if (kk < nj) {
-                    const float2 xa = jl[kk] == i ? dFa : jf[kk][ea];
-                    const float2 xb = jl[kk] == i ? dFb : jf[kk][eb];
-                    acca.x = fmaf(ja[kk], xa.x, acca.x);
-                    acca.y = fmaf(ja[kk], xa.y, acca.y);
-                    accb.x = fmaf(ja[kk], xb.x, accb.x);
-                    accb.y = fmaf(ja[kk], xb.y, accb.y);
-                  }
-                }
-                const float2 fa = ff0[ea], fb = ff0[eb];
-                if constexpr (i <= kMaxS - 2) frame(G::kDF + i)[ea] = dFa;
-                fdn[ea] = make_float2(fmaf(hcn, fa.x, acca.x), fmaf(hcn, fa.y, acca.y));
-                if (two) {
-                  if constexpr (i <= kMaxS - 2) frame(G::kDF + i)[eb] = dFb;
-                  fdn[eb] = make_float2(fmaf(hcn, fb.x, accb.x), fmaf(hcn, fb.y, accb.y));
-                }
-              }
-            } else
             for (int idx = threadIdx.x; got && idx < RQ * RQ; idx += kFusedThreads) {
               const int r = idx / RQ, c = idx - r * RQ;
               const int k = k0 - dq + r, j = j0 - dq + c;
