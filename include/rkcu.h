@@ -48,7 +48,9 @@ extern "C" {
 #define RKCU_FP64_FMA    1   /* FP64 with fused multiply-adds (fewer FP64 instructions);
                                 differs from the reference in the last bits, which can
                                 change accept/reject decisions of stiff problems */
-#define RKCU_MIXED       2   /* FP32 stage vectors, FP64 state, update and error norm */
+#define RKCU_MIXED       2   /* BRUSS2D-MIX: F0 in double-float, FP32 stage increments,
+                                FP64 state; the update and the error estimate in
+                                double-float, the error norm reduced in FP64 */
 #define RKCU_FP64_EXACT_HWMUL 3 /* RKCU_FP64_EXACT with every product on the FP64 pipe (the
                                 default exact mode computes products on the integer pipe,
                                 bit for bit the same; this one exists to compare them) */

@@ -5,11 +5,8 @@
 //
 //   stages   all chunks of all active instances, grid-stride over chunks (one
 //            CTA per chunk at a time, equal-size chunks so the stages stay
-//            balanced however uneven the instances are); before a chunk's
-//            stage i the CTA waits only for the chunks of the same instance
-//            that its stencil reaches to have finished stage i-1 (per-chunk
-//            completion marks, bounded waits); one grid barrier per sweep
-//            closes the last stage before the step control
+//            balanced however uneven the instances are); grid barrier after
+//            each stage
 //   error    per-chunk block reduction, 64-bit atomicMax into the instance
 //   control  one thread per instance: accept/reject, step size (correctly
 //            rounded pow), t, counters, next h*A (include/tools.h:191-278);
@@ -124,10 +121,7 @@ __global__ void __launch_bounds__(kT, batch_threads_per_sm<kExact>() / kT) batch
   bool ok = true;
 
   const int budget = *(volatile int *)P.budget;
-  const unsigned int sweep0 = *(volatile unsigned int *)P.sweeps;
-  int started = 0;
   for (int it = 0; it < budget; ++it) {
-    const unsigned int mark = (sweep0 + static_cast<unsigned int>(it)) * static_cast<unsigned int>(s);
     if (threadIdx.x == 0) {
       s_nch = *(volatile int *)P.nchunks;
       s_clen = *(volatile int *)P.chunk_len;
@@ -135,7 +129,6 @@ __global__ void __launch_bounds__(kT, batch_threads_per_sm<kExact>() / kT) batch
     __syncthreads();
     const int nch = s_nch, clen = s_clen;
     if (nch == 0) break;
-    started = it + 1;
 
     for (int i = 0; i < s && ok; ++i) {
       const bool last = (i == s - 1);
@@ -143,19 +136,6 @@ __global__ void __launch_bounds__(kT, batch_threads_per_sm<kExact>() / kT) batch
         const int2 ch = P.chunks[c];
         const InstDesc &d = P.desc[ch.x];
         if (d.pending) continue;  // waits for its step size from the host (same for every CTA)
-        if (i > 0) {
-          // the instance's chunks within its stencil's reach (a grid row for
-          // BRUSS2D-MIX) must have finished stage i-1
-          const int dep = d.kind == RKCU_PROBLEM_BRUSS2D_MIX ? d.grid_n
-                          : d.kind == RKCU_PROBLEM_LV_BANDED  ? 1
-                                                              : 0;
-          const int first = c - ch.y / clen;
-          const int last = first + (d.npairs + clen - 1) / clen - 1;
-          const int reach = (dep + clen - 1) / clen;
-          if (!(ok = wait_tiles(P.chunk_done, max(first, c - reach), min(last, c + reach), mark + i, st,
-                                P.timeout_ns, 20 + i)))
-            break;
-        }
         const InstCoef &K = P.coef[ch.x];
         const size_t np = static_cast<size_t>(d.npairs);
         double2 *__restrict__ vec = d.vec;
@@ -217,7 +197,6 @@ __global__ void __launch_bounds__(kT, batch_threads_per_sm<kExact>() / kT) batch
             }
           }
         }
-        if (!last) publish_tile(P.chunk_done, c, mark + i + 1);
         if (last) {
           double emax = em.best;
 #pragma unroll
@@ -233,10 +212,9 @@ __global__ void __launch_bounds__(kT, batch_threads_per_sm<kExact>() / kT) batch
           __syncthreads();
         }
       }
-      if (!ok) break;
+      ok = grid_barrier(st, P.nblocks, P.timeout_ns, 20 + i);
     }
     if (!ok) break;
-    if (!(ok = grid_barrier(st, P.nblocks, P.timeout_ns, 20 + s))) break;
 
     // step control, one thread per instance (include/tools.h:191-278)
     const int nslots = *(volatile int *)P.nslots;
@@ -314,9 +292,6 @@ __global__ void __launch_bounds__(kT, batch_threads_per_sm<kExact>() / kT) batch
       // by all after the next barrier
     }
   }
-  // sweeps started in this launch (a sweep cut short by an error counts, so the
-  // next launch's marks stay above every mark written so far)
-  if (blockIdx.x == 0 && threadIdx.x == 0) *P.sweeps = sweep0 + static_cast<unsigned int>(started);
 }
 
 cudaError_t launch_batch_rebuild(const BatchParams &p, cudaStream_t stream) {

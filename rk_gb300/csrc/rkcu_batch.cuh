@@ -64,11 +64,6 @@ struct BatchParams {
   unsigned long long timeout_ns;
   DevState *st;        // barrier words and error flag
   PowBox *pow_box;     // one mailbox per slot (device view of mapped host memory)
-  // Stage completion per chunk: chunk_done[c] = sweep * s + i + 1 once stage i of
-  // chunk c is written; sweeps counts every sweep since the batch was created
-  // (device word, carried across launches), so marks only grow.
-  unsigned int *chunk_done;
-  unsigned int *sweeps;
 };
 
 cudaError_t launch_batch_rebuild(const BatchParams &p, cudaStream_t stream);

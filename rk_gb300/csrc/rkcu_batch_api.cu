@@ -52,8 +52,7 @@ struct rkcu_batch {
   int2 *d_chunks = nullptr;
   size_t chunk_cap = 0;
   int *d_ints = nullptr;  // [0] nslots, [1] nchunks, [2] rebuild, [3] done_count, [4] chunk
-                          // length, [5] sweeps of the next launch, [6] sweeps so far
-  unsigned int *d_chunk_done = nullptr;  // per-chunk stage completion marks
+                          // length, [5] sweeps of the next launch
   int *d_done = nullptr;
   DevState *d_st = nullptr;
   rkcu::PowBox *h_box = nullptr;  // mapped, pinned host memory: one mailbox per slot
@@ -146,8 +145,6 @@ BatchParams make_params(rkcu_batch *b) {
   p.chunks = b->d_chunks;
   p.chunk_pairs = b->chunk_pairs;
   p.budget = b->d_ints + 5;
-  p.sweeps = reinterpret_cast<unsigned int *>(b->d_ints + 6);
-  p.chunk_done = b->d_chunk_done;
   p.timeout_ns = (unsigned long long)(b->opt.wait_timeout_s * 1e9);
   p.st = b->d_st;
   p.pow_box = b->d_box;
@@ -331,12 +328,8 @@ int rkcu_batch_create(rkcu_batch **out, long long arena_bytes, int max_instances
   b->chunk_cap = b->arena_bytes / (sizeof(double2) * 128) + (size_t)max_instances + 1;
   if ((e = cudaMalloc(&b->d_chunks, sizeof(int2) * b->chunk_cap)) != cudaSuccess)
     return bail(fail(b, e, "chunks"));
-  if ((e = cudaMalloc(&b->d_ints, 7 * sizeof(int))) != cudaSuccess) return bail(fail(b, e, "ints"));
-  if ((e = cudaMemset(b->d_ints, 0, 7 * sizeof(int))) != cudaSuccess) return bail(fail(b, e, "ints"));
-  if ((e = cudaMalloc(&b->d_chunk_done, sizeof(unsigned int) * b->chunk_cap)) != cudaSuccess)
-    return bail(fail(b, e, "chunk marks"));
-  if ((e = cudaMemset(b->d_chunk_done, 0, sizeof(unsigned int) * b->chunk_cap)) != cudaSuccess)
-    return bail(fail(b, e, "chunk marks"));
+  if ((e = cudaMalloc(&b->d_ints, 6 * sizeof(int))) != cudaSuccess) return bail(fail(b, e, "ints"));
+  if ((e = cudaMemset(b->d_ints, 0, 6 * sizeof(int))) != cudaSuccess) return bail(fail(b, e, "ints"));
   if ((e = cudaMalloc(&b->d_done, sizeof(int) * max_instances)) != cudaSuccess)
     return bail(fail(b, e, "done list"));
   if ((e = cudaMalloc(&b->d_st, sizeof(DevState))) != cudaSuccess) return bail(fail(b, e, "state"));
@@ -362,7 +355,6 @@ int rkcu_batch_destroy(rkcu_batch *b) {
   cudaFree(b->d_chunks);
   cudaFree(b->d_ints);
   cudaFree(b->d_done);
-  cudaFree(b->d_chunk_done);
   cudaFree(b->d_st);
   if (b->h_box) cudaFreeHost(b->h_box);
   if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
