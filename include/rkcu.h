@@ -167,7 +167,9 @@ int rkcu_solve(rkcu_solver *s, double t0, double te, const double *y0, double *y
              pointer if y0_on_device == 0, else a device pointer)
    advance-- enqueue up to max_steps attempted steps on the solver's stream (async);
              the device stops by itself at te, at the step limit, or after a step
-             whose size update is left to the host (see rkcu_step_size)
+             whose size update is left to the host (see rkcu_step_size; rkcu_run and
+             rkcu_solve answer such updates while the launch runs, so their launches
+             go on)
    query  -- wait for the stream, finish such an update, read the counters
    get_y  -- copy the current y out (host or device destination) */
 int rkcu_begin(rkcu_solver *s, double t0, double te, const double *y0, int y0_on_device,

@@ -102,6 +102,9 @@ struct rkcu_solver {
   double *lv_r = nullptr, *lv_a = nullptr;
   DevState *st = nullptr;
   DevState *st_host = nullptr;  // pinned
+  rkcu::PowBox *h_box = nullptr;  // step-size mailbox, mapped pinned host memory
+  rkcu::PowBox *d_box = nullptr;  // its device address
+  bool polling = false;           // the calling thread answers the mailbox (rkcu_run, rkcu_solve)
   unsigned int *flags = nullptr;  // plain kernel: per-CTA stage progress
   // per-step trace (plain form)
   int trace_cap = 0;
@@ -235,6 +238,7 @@ int rkcu_destroy(rkcu_solver *s) {
   cudaFree(s->trace_meta);
   cudaFree(s->trace_y);
   cudaFreeHost(s->st_host);
+  if (s->h_box) cudaFreeHost(s->h_box);
   if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
   delete s;
   return RKCU_OK;
@@ -300,6 +304,12 @@ int rkcu_create(rkcu_solver **out, const rkcu_problem *prob, const rkcu_options 
     return fail(cuda_fail(e, "cudaMalloc state"));
   if ((e = cudaMallocHost(&s->st_host, sizeof(DevState))) != cudaSuccess)
     return fail(cuda_fail(e, "cudaMallocHost"));
+  if ((e = cudaHostAlloc(&s->h_box, sizeof(rkcu::PowBox), cudaHostAllocMapped | cudaHostAllocPortable)) !=
+      cudaSuccess)
+    return fail(cuda_fail(e, "step-size mailbox"));
+  std::memset(s->h_box, 0, sizeof(rkcu::PowBox));
+  if ((e = cudaHostGetDevicePointer(&s->d_box, s->h_box, 0)) != cudaSuccess)
+    return fail(cuda_fail(e, "step-size mailbox"));
   {
     int tile = 0, ntiles = 0, dep = 0;
     flow_geometry(s, &tile, &ntiles, &dep);
@@ -445,6 +455,7 @@ int rkcu_begin(rkcu_solver *s, double t0, double te, const double *y0, int y0_on
   const double h0 = s->opt.h_init > 0.0 ? s->opt.h_init : tol > 0.0 ? std::fmin(10.0 * tol, lim) : lim;
   DevState *h = s->st_host;
   std::memset(h, 0, sizeof(*h));
+  s->h_box->req = s->h_box->ans = 0;  // no kernel that uses it runs now (rkcu_run waits for its own)
   h->t = t0;
   h->h = h0;
   h->cur = 0;
@@ -605,6 +616,7 @@ int rkcu_advance(rkcu_solver *s, int max_steps) {
   p.trace_cap = s->trace_cap;
   p.trace_meta = s->trace_meta;
   p.trace_y = s->trace_y;
+  p.pow_box = s->polling ? s->d_box : nullptr;
   p.bruss.N = s->prob.grid_n;
   p.bruss.coef = s->prob.problem == RKCU_PROBLEM_BRUSS2D_MIX ? bruss_coef(&s->prob) : 0.0;
   p.lvb.n = s->prob.n;
@@ -672,6 +684,33 @@ int rkcu_get_y(rkcu_solver *s, double *y, int y_on_device) {
   return RKCU_OK;
 }
 
+// Answer a step-size update the running plain kernel posted to the mailbox:
+// include/tools.h:221-233 with the C library's pow, exactly as rkcu_query
+// finishes a pending update.
+static void answer_mailbox(rkcu_solver *s) {
+  rkcu::PowBox &x = *s->h_box;
+  const unsigned req = __atomic_load_n(&x.req, __ATOMIC_ACQUIRE);
+  if (req == x.ans) return;
+  x.h_new = x.h * std::fmin(2.0, std::fmax(0.5, 0.9 * std::pow(s->tol / x.err, 1.0 / (s->ord + 1.0))));
+  __atomic_store_n(&x.ans, req, __ATOMIC_RELEASE);
+}
+
+// One launch of up to max_steps steps while this thread answers the mailbox,
+// then the counters (the launches that poll: rkcu_run and rkcu_solve).
+static int advance_polling(rkcu_solver *s, int max_steps, rkcu_stats *st) {
+  s->polling = true;
+  int rc = rkcu_advance(s, max_steps);
+  s->polling = false;
+  if (rc != RKCU_OK) return rc;
+  for (;;) {
+    answer_mailbox(s);
+    const cudaError_t q = cudaStreamQuery(s->stream);
+    if (q == cudaSuccess) break;
+    if (q != cudaErrorNotReady) return cuda_fail(q, "step loop");
+  }
+  return rkcu_query(s, st);
+}
+
 int rkcu_solve(rkcu_solver *s, double t0, double te, const double *y0, double *y, double tol,
                rkcu_stats *stats) {
   if (!s || !y0 || !y) return RKCU_ERR_INVALID;
@@ -679,10 +718,8 @@ int rkcu_solve(rkcu_solver *s, double t0, double te, const double *y0, double *y
   if (rc != RKCU_OK) return rc;
   rkcu_stats st{};
   if ((rc = rkcu_query(s, &st)) != RKCU_OK) return rc;
-  while (!st.done) {
-    if ((rc = rkcu_advance(s, 1 << 20)) != RKCU_OK) return rc;
-    if ((rc = rkcu_query(s, &st)) != RKCU_OK) return rc;
-  }
+  while (!st.done)
+    if ((rc = advance_polling(s, 1 << 20, &st)) != RKCU_OK) return rc;
   if ((rc = rkcu_get_y(s, y, 0)) != RKCU_OK) return rc;
   if (stats) *stats = st;
   return RKCU_OK;
@@ -697,8 +734,7 @@ int rkcu_run(rkcu_solver *s, int max_steps, rkcu_stats *stats) {
   const long long target = (long long)st.steps_acc + st.steps_rej + (max_steps > 0 ? max_steps : 0);
   while (!st.done && (long long)st.steps_acc + st.steps_rej < target) {
     const long long left = target - st.steps_acc - st.steps_rej;
-    if ((rc = rkcu_advance(s, (int)(left < (1 << 30) ? left : (1 << 30)))) != RKCU_OK) return rc;
-    if ((rc = rkcu_query(s, &st)) != RKCU_OK) return rc;
+    if ((rc = advance_polling(s, (int)(left < (1 << 30) ? left : (1 << 30)), &st)) != RKCU_OK) return rc;
   }
   if (stats) *stats = st;
   return RKCU_OK;

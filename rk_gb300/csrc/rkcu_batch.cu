@@ -25,16 +25,6 @@
 
 namespace rkcu {
 
-// System-scope release store / acquire load of a word in mapped host memory.
-__device__ __forceinline__ void st_release_sys(unsigned int *p, unsigned int v) {
-  asm volatile("st.release.sys.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-__device__ __forceinline__ unsigned int ld_acquire_sys(const unsigned int *p) {
-  unsigned int v;
-  asm volatile("ld.acquire.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-
 template <int kExact>
 __device__ __forceinline__ double2 batch_rhs(const InstDesc &d, const double2 *w, int p) {
   switch (d.kind) {

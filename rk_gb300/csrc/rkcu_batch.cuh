@@ -27,14 +27,6 @@ struct InstDesc {
   unsigned int pend_seq;
 };
 
-// Mailbox of one slot in mapped, pinned host memory: the kernel posts the
-// error max and step size of a step whose size update is left to the host
-// (req = sequence number, written last with release semantics); the host
-// answers with the new step size (ans = req, written last).
-struct PowBox {
-  unsigned int req, ans;
-  double err, h, h_new;
-};
 
 // h*A, h*b, h*(b - b^) of the running step, one per slot (device memory)
 struct InstCoef {

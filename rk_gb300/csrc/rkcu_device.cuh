@@ -252,7 +252,32 @@ struct DevState {
   double pend_err;    // the step's error max
   double pend_h;      // the step's h
   long long host_pow_steps;  // how many updates the host finished so far
+  // Updates answered through the mailbox while the kernel runs (PowBox): the
+  // sequence number of the last one posted, whether its answer came in time,
+  // and the answer.
+  unsigned int host_seq;
+  int host_answered;
+  double host_h;
 };
+
+// Mailbox in mapped, pinned host memory for a step-size update left to the
+// host: the kernel posts the step's error max and step size (req = sequence
+// number, written last with release semantics); the host answers with the new
+// step size (ans = req, written last).
+struct PowBox {
+  unsigned int req, ans;
+  double err, h, h_new;
+};
+
+// System-scope release store / acquire load of a word in mapped host memory.
+__device__ __forceinline__ void st_release_sys(unsigned int *p, unsigned int v) {
+  asm volatile("st.release.sys.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned int ld_acquire_sys(const unsigned int *p) {
+  unsigned int v;
+  asm volatile("ld.acquire.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
 
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
   unsigned long long t;

@@ -37,6 +37,8 @@ constexpr int kThreads = 256;
 // stage input's grid rows staged in a ring of kRingSlots rows of shared memory.
 constexpr int kRingThreads = 1024;
 constexpr int kRingSlots = 4;
+// How long CTA 0 waits for the host's answer to a posted step-size update.
+constexpr unsigned long long kHostAnswerNs = 2000000ull;
 // Chunks of blockDim pairs by which the L2 bulk prefetch runs ahead (0: off).
 constexpr int kL2Ahead = 0;
 
@@ -512,6 +514,35 @@ __global__ void __launch_bounds__(kRing ? kRingThreads : kThreads, kRing ? 1 : p
       s_step = s_step + 1;
     }
     __syncthreads();
+    if (s_pending && P.pow_box) {
+      // The host polls the mailbox while this launch runs: CTA 0 posts the
+      // update and waits a short, bounded time for the C library's pow; the
+      // grid barrier hands the answer to every CTA.  Without an answer in time
+      // the launch ends as below and the host finishes the update after it.
+      if (blockIdx.x == 0 && threadIdx.x == 0) {
+        PowBox *box = P.pow_box;
+        const unsigned int seq = st->host_seq + 1;
+        st->host_seq = seq;
+        *(volatile double *)&box->err = s_pend_err;
+        *(volatile double *)&box->h = s_pend_h;
+        st_release_sys(&box->req, seq);
+        const unsigned long long t0 = globaltimer_ns();
+        bool got = false;
+        while (!(got = ld_acquire_sys(&box->ans) == seq) && globaltimer_ns() - t0 < kHostAnswerNs)
+          __nanosleep(64);
+        st->host_h = got ? *(volatile double *)&box->h_new : 0.0;
+        st->host_answered = got ? 1 : 0;
+        if (got) ++st->host_pow_steps;
+      }
+      if (!(ok = grid_barrier(st, P.nblocks, P.timeout_ns, 7))) break;
+      if (threadIdx.x == 0 && *(volatile int *)&st->host_answered) {
+        // as the host would finish it: the loop increment and test of tools.h:196-197
+        s_h = fmin(*(volatile double *)&st->host_h, P.te - s_t);
+        s_done = !(s_t < P.te) || (P.step_limit > 0 && s_acc + s_rej >= P.step_limit);
+        s_pending = 0;
+      }
+      __syncthreads();
+    }
     if (s_pending) break;  // the host finishes this step's size update
   }
 

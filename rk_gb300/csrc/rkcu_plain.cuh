@@ -41,6 +41,10 @@ struct PlainParams {
   int trace_cap;
   double *trace_meta;
   double2 *trace_y;
+  // Mailbox for step-size updates left to the host (device view of mapped host
+  // memory), set only while the host polls it; null: such an update ends the
+  // launch and the host finishes it before the next one.
+  PowBox *pow_box;
   Bruss bruss;
   LvPairs lvp;
   LvBanded lvb;
