@@ -39,8 +39,6 @@ constexpr int kRingThreads = 1024;
 constexpr int kRingSlots = 4;
 // How long CTA 0 waits for the host's answer to a posted step-size update.
 constexpr unsigned long long kHostAnswerNs = 2000000ull;
-// Chunks of blockDim pairs by which the L2 bulk prefetch runs ahead (0: off).
-constexpr int kL2Ahead = 0;
 
 template <class Prob>
 __device__ __forceinline__ const Prob &problem_of(const PlainParams &P);
@@ -274,46 +272,6 @@ __global__ void __launch_bounds__(kRing ? kRingThreads : kThreads, kRing ? 1 : p
         pf(&ycur[q]);
       }
     };
-    // Bulk prefetch into L2 (the TMA unit's cp.async.bulk.prefetch) of the
-    // chunk kL2Ahead chunks ahead of this CTA's current one, for every vector
-    // the stage reads there (and the stencil's next grid row); issued by one
-    // thread per chunk.  kL2Ahead = 0 leaves it out.
-    auto l2_chunk = [&](const double2 *v, int q0, int limit) {
-      if constexpr (kL2Ahead > 0) {
-        const int q = q0 + kL2Ahead * pstep;
-        if (q < limit) {
-          const int cnt = min(static_cast<int>(blockDim.x), limit - q);
-          asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(v + q),
-                       "r"(static_cast<unsigned>(cnt) * 16u)
-                       : "memory");
-        }
-      }
-    };
-    // a stage input's chunk and the chunk one grid row further (the stencil's next row)
-    auto l2_stencil = [&](const double2 *v, int q0) {
-      l2_chunk(v, q0, pend);
-      l2_chunk(v + rowN, q0, P.npairs - rowN);
-    };
-    auto l2_first = [&](int q0) {
-      if (kL2Ahead > 0 && threadIdx.x == 0) l2_stencil(ycur, q0);
-    };
-    auto l2_mid = [&](int i, int q0) {
-      if (kL2Ahead > 0 && threadIdx.x == 0) {
-        l2_stencil(P.w[i], q0);
-        for (int l = i + 1; l < s; ++l)
-          if (P.nzA[l * kMaxStages + i]) l2_chunk(P.w[l], q0, pend);
-        if (P.nzb[i]) l2_chunk(P.dy, q0, pend);
-        if (P.nzbh[i]) l2_chunk(P.err, q0, pend);
-      }
-    };
-    auto l2_last = [&](int q0) {
-      if (kL2Ahead > 0 && threadIdx.x == 0) {
-        l2_stencil(P.w[s - 1], q0);
-        l2_chunk(P.dy, q0, pend);
-        l2_chunk(P.err, q0, pend);
-        l2_chunk(ycur, q0, pend);
-      }
-    };
     if (P.schedule == kScheduleFlow) {
       // Dataflow over (stage, tile) tickets in skewed wavefront order: tile c
       // of stage i is ticket (c + K i) s + i, and waits only until stage i-1
@@ -436,14 +394,12 @@ __global__ void __launch_bounds__(kRing ? kRingThreads : kThreads, kRing ? 1 : p
     } else {
       for (GridCursor g(p0, rowN); g.p < pend; g.advance(pstep, dk_s, dj_s, rowN)) {
         pf_first(g.p + pstep);
-        l2_first(g.p);
         stage_first(g.p, g.k, g.j);
       }
       if (!(ok = stage_sync(P, c_lo, c_hi, ++progress, 1))) break;
       for (int i = 1; i < s - 1; ++i) {
         for (GridCursor g(p0, rowN); g.p < pend; g.advance(pstep, dk_s, dj_s, rowN)) {
           pf_mid(i, g.p + pstep);
-          l2_mid(i, g.p);
           stage_mid(i, g.p, g.k, g.j);
         }
         if (!(ok = stage_sync(P, c_lo, c_hi, ++progress, 2))) break;
@@ -451,7 +407,6 @@ __global__ void __launch_bounds__(kRing ? kRingThreads : kThreads, kRing ? 1 : p
       if (!ok) break;
       for (GridCursor g(p0, rowN); g.p < pend; g.advance(pstep, dk_s, dj_s, rowN)) {
         pf_last(g.p + pstep);
-        l2_last(g.p);
         stage_last(g.p, g.k, g.j);
       }
     }
