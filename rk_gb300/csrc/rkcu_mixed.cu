@@ -173,13 +173,13 @@ __device__ __forceinline__ double2 mix_update(const float2 (&d)[kMaxS], float2 d
   return yn;
 }
 
-// Fused FP32 stages: all stages 1 .. s-1 of a step on one tile of kFT x kFT
+// Fused FP32 stages: all stages 1 .. s-1 of a step on one tile of kFTR x kFTC
 // grid points in shared memory.  Stage i is evaluated on the tile and a halo
 // of s-1-i points (its increments are read one point further out by the next
 // stage's stencil), so the last stage needs the tile alone; only F0 and y32
 // (with a halo of s-1 points) are read from memory, one TMA box each,
 // double-buffered, and only y_new is written.
-constexpr int kFT = 32;
+constexpr int kFTR = 32, kFTC = 32;  // tile rows, columns
 constexpr int kFusedThreads = 1024;
 constexpr int mix_threads(int path) { return path == kMixFused ? kFusedThreads : kMixThreads; }
 
@@ -188,7 +188,7 @@ struct FusedGeom {
   static constexpr int HY = kS - 1;                       // row halo
   static constexpr int HX = (kS - 1 + 1) / 2 * 2;         // column halo, even: a TMA box
                                                           // must start on 16 bytes
-  static constexpr int FR = kFT + 2 * HY, FC = kFT + 2 * HX;  // frame rows, columns
+  static constexpr int FR = kFTR + 2 * HY, FC = kFTC + 2 * HX;  // frame rows, columns
   static constexpr int kFrame = FR * FC;                  // points (float2) per frame
   static constexpr unsigned kFrameBytes = (kFrame * 8u + 127u) / 128u * 128u;
   // F0 and y32 twice (double buffer), delta twice (this stage's and the
@@ -223,7 +223,7 @@ static __device__ __noinline__ void stage0_point_fp64(const Bruss &br, const dou
 // kMaxS: an upper bound of the stage count (8 or 13), so that the per-stage
 // loops over earlier stages unroll; kPath: how the FP32 stages walk the grid.
 template <int kMaxS, int kPath>
-__global__ void __launch_bounds__(mix_threads(kPath), kPath == kMixFused ? 1 : (kMaxS <= 8 ? 4 : 2))
+__global__ void __launch_bounds__(mix_threads(kPath), kPath == kMixFused ? 1024 / kFusedThreads : (kMaxS <= 8 ? 4 : 2))
     mixed_kernel(const __grid_constant__ MixedParams P) {
   // TMA staging buffers: 2 (double buffer) x s slots of kSlotBytes, from the
   // first 128-byte boundary of the dynamic shared memory (128 bytes spare)
@@ -352,10 +352,10 @@ __global__ void __launch_bounds__(mix_threads(kPath), kPath == kMixFused ? 1 : (
       // double-buffered; delta_i and dF_i in shared-memory frames.
       using G = FusedGeom<kMaxS>;
       auto frame = [&](int f) { return reinterpret_cast<float2 *>(s_box + static_cast<size_t>(f) * G::kFrameBytes); };
-      const int tiles_x = (N + kFT - 1) / kFT;
-      const int ntiles = tiles_x * tiles_x;
+      const int tiles_x = (N + kFTC - 1) / kFTC;
+      const int ntiles = tiles_x * ((N + kFTR - 1) / kFTR);
       auto issue = [&](int t, int b) {
-        const int k0 = (t / tiles_x) * kFT, j0 = (t % tiles_x) * kFT;
+        const int k0 = (t / tiles_x) * kFTR, j0 = (t % tiles_x) * kFTC;
         mbar_arrive_expect_tx(&s_mbar[b], 2u * G::kFrame * 8u);
         tma_load_2d(frame(2 * b), &P.tm[0], 2 * (j0 - G::HX), k0 - G::HY, &s_mbar[b]);
         tma_load_2d(frame(2 * b + 1), &P.tm[1], 2 * (j0 - G::HX), k0 - G::HY, &s_mbar[b]);
@@ -383,13 +383,13 @@ __global__ void __launch_bounds__(mix_threads(kPath), kPath == kMixFused ? 1 : (
           phase ^= 1u << b;
           pending &= ~(1u << b);
         }
-        const int k0 = (t / tiles_x) * kFT, j0 = (t % tiles_x) * kFT;
+        const int k0 = (t / tiles_x) * kFTR, j0 = (t % tiles_x) * kFTC;
         const float2 *const ff0 = frame(2 * b), *const fy32 = frame(2 * b + 1);
         // A tile whose regions lie inside the grid away from its edges (all but
         // the outermost ring of tiles) needs no bounds checks and no boundary
         // stencils: its loops are compiled without them.
-        const bool interior = k0 >= kMaxS - 1 && j0 >= kMaxS - 1 && k0 + kFT + kMaxS - 1 <= N &&
-                              j0 + kFT + kMaxS - 1 <= N;
+        const bool interior = k0 >= kMaxS - 1 && j0 >= kMaxS - 1 && k0 + kFTR + kMaxS - 1 <= N &&
+                              j0 + kFTC + kMaxS - 1 <= N;
         auto stages = [&](auto interior_c) {
           constexpr bool kIn = decltype(interior_c)::value;
           // One pass per stage i over the tile and a halo of s-1-i points:
@@ -399,7 +399,7 @@ __global__ void __launch_bounds__(mix_threads(kPath), kPath == kMixFused ? 1 : (
           static_for<1, kMaxS>([&](auto ic) {
             constexpr int i = decltype(ic)::value;
             constexpr bool kLast = i == kMaxS - 1;
-            constexpr int dq = kMaxS - 1 - i, RQ = kFT + 2 * dq;
+            constexpr int dq = kMaxS - 1 - i, RQ = kFTC + 2 * dq, RR = kFTR + 2 * dq;  // region cols, rows
             constexpr int eb_q = (G::HY - dq) * G::FC + (G::HX - dq);
             constexpr int kJ = i;  // delta_{i+1} sums over j = 1 .. i
             const float2 *const fdi = i == 1 ? ff0 : frame(G::kDelta + (i & 1));
@@ -416,7 +416,7 @@ __global__ void __launch_bounds__(mix_threads(kPath), kPath == kMixFused ? 1 : (
               ja[kk] = kk < nj ? s_ja[i + 1][kk] : 0.0f;
               jf[kk] = frame(G::kDF + (jl[kk] >= 1 && jl[kk] < i ? jl[kk] : 1));
             }
-            for (int idx = threadIdx.x; got && idx < RQ * RQ; idx += kFusedThreads) {
+            for (int idx = threadIdx.x; got && idx < RR * RQ; idx += kFusedThreads) {
               const int r = idx / RQ, c = idx - r * RQ;
               const int k = k0 - dq + r, j = j0 - dq + c;
               const int e = eb_q + r * G::FC + c;
@@ -758,8 +758,7 @@ cudaError_t launch_mixed(const MixedParams &p, int path, int num_sms, cudaStream
     kern = f.kern;
     dyn = f.smem;
     threads = kFusedThreads;
-    const int tiles_x = (p.bruss.N + kFT - 1) / kFT;
-    useful = tiles_x * tiles_x;
+    useful = ((p.bruss.N + kFTC - 1) / kFTC) * ((p.bruss.N + kFTR - 1) / kFTR);
   } else {
     q.path = kMixTiles;
     if (path == kMixTilesTma && p.s <= kMixTmaStages) {
