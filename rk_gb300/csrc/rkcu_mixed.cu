@@ -179,8 +179,8 @@ __device__ __forceinline__ double2 mix_update(const float2 (&d)[kMaxS], float2 d
 // stage's stencil), so the last stage needs the tile alone; only F0 and y32
 // (with a halo of s-1 points) are read from memory, one TMA box each,
 // double-buffered, and only y_new is written.
-constexpr int kFTR = 32, kFTC = 32;  // tile rows, columns
-constexpr int kFusedThreads = 1024;
+constexpr int kFTR = 16, kFTC = 32;  // tile rows, columns
+constexpr int kFusedThreads = 512;   // two CTAs per SM
 constexpr int mix_threads(int path) { return path == kMixFused ? kFusedThreads : kMixThreads; }
 
 template <int kS>
