@@ -215,6 +215,33 @@ SFP_HD double add(double a, double b) {
   return double_of(sign | ((static_cast<uint64_t>(e - 1) << 52) + m));
 }
 
+// The high 64 bits of the 128-bit product a * b.
+SFP_HD uint64_t mul_hi64(uint64_t a, uint64_t b) {
+#ifdef __CUDA_ARCH__
+  return __umul64hi(a, b);
+#else
+  return static_cast<uint64_t>((static_cast<unsigned __int128>(a) * b) >> 64);
+#endif
+}
+
+// Whether a / d > r holds exactly, for positive normal doubles given as bit
+// patterns, decided as a > r d with the 106-bit product of the significands in
+// integers: no division and no FP64 instruction.  Rounding to nearest is
+// monotonic, so a quotient that does not exceed r exactly cannot round above
+// it, and the caller divides only when this returns true.
+//   a = ma 2^(ea-1075), r d = mr md 2^(er+ed-2150):  a > r d  <=>  ma 2^t > mr md,
+//   t = ea + 1075 - er - ed, with ma 2^t in [2^(52+t), 2^(53+t)) and mr md in [2^104, 2^106).
+SFP_HD bool quotient_exceeds(uint64_t ba, uint64_t bd, uint64_t br) {
+  constexpr uint64_t kF = 0x000fffffffffffffull, kH = 0x0010000000000000ull;
+  const int t = static_cast<int>(ba >> 52) + 1075 - static_cast<int>(bd >> 52) - static_cast<int>(br >> 52);
+  if (t >= 54) return true;
+  if (t <= 51) return false;
+  const uint64_t ma = (ba & kF) | kH, md = (bd & kF) | kH, mr = (br & kF) | kH;
+  const uint64_t lhi = ma >> (64 - t), llo = ma << t;  // t is 52 or 53
+  const uint64_t phi = mul_hi64(mr, md), plo = mr * md;
+  return lhi > phi || (lhi == phi && llo > plo);
+}
+
 // s rounded to a multiple of 2^k (k = 1, 2), ties to an even multiple of 2^k:
 // the rounding of a sum of same-binade significands to the binade above.
 SFP_HD uint64_t round_units(uint64_t s, int k) {

@@ -1,5 +1,6 @@
-// Bit-exactness check of the software binary64 multiply/add (rkcu_softfp64.cuh)
-// against the host's IEEE round-to-nearest arithmetic.  Compiled with
+// Bit-exactness check of the software binary64 multiply/add, the same-binade
+// Laplacian and the exact quotient test (rkcu_softfp64.cuh) against the host's
+// IEEE round-to-nearest arithmetic.  Compiled with
 // -ffp-contract=off.  Usage: softfp64_check <count> <seed>; prints mismatches.
 #include <cinttypes>
 #include <cmath>
@@ -119,5 +120,41 @@ int main(int argc, char **argv) {
     }
   }
   printf("lap mismatches %lld (fast path taken %lld of %lld)\n", bad_lap, taken, count);
-  return (bad_mul || bad_add || bad_cvt || bad_lap) ? 1 : 0;
+
+  // the exact quotient test a / d > r against the product and its FMA error
+  // term (r d = p + err exactly in this exponent range): random operands, r
+  // the rounded quotient and its neighbours, and exactly representable
+  // quotients (few-bit significands, a = r d) with their neighbours
+  long long bad_quot = 0, above = 0;
+  for (long long i = 0; i < count; ++i) {
+    const uint64_t r0 = next(), r1 = next(), r2 = next();
+    auto band = [](uint64_t q, int lo, int span) {
+      return double_of((q & 0x000fffffffffffffull) | (static_cast<uint64_t>(1023 + lo + static_cast<int>((q >> 52) % span)) << 52));
+    };
+    double a = band(r0, -300, 600), d = band(r1, -300, 600), r;
+    switch (r2 % 4) {
+      case 0: r = band(r2, -300, 600); break;
+      case 1: r = double_of(bits_of(a / d) + (static_cast<int64_t>((r2 >> 8) % 5) - 2)); break;
+      case 2: {  // a / d exactly representable
+        d = double_of(bits_of(d) & ~0x000000ffffffffffull);
+        r = double_of(bits_of(band(r2, -300, 600)) & ~0x000000ffffffffffull);
+        a = r * d;
+        r = double_of(bits_of(r) + (static_cast<int64_t>((r2 >> 8) % 3) - 1));
+        break;
+      }
+      default: {  // a next to a representable r d
+        d = double_of(bits_of(d) & ~0x000000ffffffffffull);
+        r = double_of(bits_of(band(r2, -300, 600)) & ~0x000000ffffffffffull);
+        a = double_of(bits_of(r * d) + (static_cast<int64_t>((r2 >> 8) % 3) - 1));
+        break;
+      }
+    }
+    const double p = r * d, err = std::fma(r, d, -p);
+    const bool want = a > p || (a == p && err < 0.0);
+    const bool got = rkcu::softfp::quotient_exceeds(bits_of(a), bits_of(d), bits_of(r));
+    above += want;
+    if (got != want && bad_quot++ < 5) printf("quotient %a / %a > %a: want %d got %d\n", a, d, r, want, got);
+  }
+  printf("quotient mismatches %lld (exceeding %lld of %lld)\n", bad_quot, above, count);
+  return (bad_mul || bad_add || bad_cvt || bad_lap || bad_quot) ? 1 : 0;
 }

@@ -1,7 +1,7 @@
 // Device check of the software binary64 multiply/add, double -> float
-// rounding and the same-binade Laplacian (rkcu_softfp64.cuh) against the FP64
-// pipe's __dmul_rn/__dadd_rn/__fma_rn/__double2float_rn on random and
-// adversarial operands.  Usage: softfp64_check_gpu <count> <seed>; prints mismatches.
+// rounding, the same-binade Laplacian and the exact quotient test
+// (rkcu_softfp64.cuh) against the FP64 pipe's __dmul_rn/__dadd_rn/__fma_rn/
+// __double2float_rn on random and adversarial operands.  Usage: softfp64_check_gpu <count> <seed>; prints mismatches.
 #include <cstdio>
 #include <cstdlib>
 
@@ -96,17 +96,58 @@ __global__ void check_lap(long long count, unsigned long long seed, unsigned lon
   atomicAdd(&bad[4], taken);
 }
 
+// the exact quotient test a / d > r against the product and its FMA error term
+// (r d = p + err exactly in this exponent range), on the device: random
+// operands, r the rounded quotient and its neighbours, exactly representable
+// quotients and their neighbours
+__device__ double band(uint64_t q) {
+  return double_of((q & 0x000fffffffffffffull) | ((uint64_t)(1023 - 300 + (int)((q >> 52) % 600)) << 52));
+}
+
+__global__ void check_quot(long long count, unsigned long long seed, unsigned long long *bad) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  unsigned long long bq = 0, above = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += stride) {
+    const uint64_t r0 = mix(seed + 3 * i + 11), r1 = mix(seed + 3 * i + 12), r2 = mix(seed + 3 * i + 13);
+    double a = band(r0), d = band(r1), r;
+    const uint64_t low40 = 0x000000ffffffffffull;
+    switch (r2 % 4) {
+      case 0: r = band(r2); break;
+      case 1: r = double_of(bits_of(__ddiv_rn(a, d)) + ((int64_t)((r2 >> 8) % 5) - 2)); break;
+      case 2:
+        d = double_of(bits_of(d) & ~low40);
+        r = double_of(bits_of(band(r2)) & ~low40);
+        a = __dmul_rn(r, d);
+        r = double_of(bits_of(r) + ((int64_t)((r2 >> 8) % 3) - 1));
+        break;
+      default:
+        d = double_of(bits_of(d) & ~low40);
+        r = double_of(bits_of(band(r2)) & ~low40);
+        a = double_of(bits_of(__dmul_rn(r, d)) + ((int64_t)((r2 >> 8) % 3) - 1));
+        break;
+    }
+    const double p = __dmul_rn(r, d), err = __fma_rn(r, d, -p);
+    const bool want = a > p || (a == p && err < 0.0);
+    above += want;
+    if (quotient_exceeds(bits_of(a), bits_of(d), bits_of(r)) != want) ++bq;
+  }
+  if (bq) atomicAdd(&bad[5], bq);
+  atomicAdd(&bad[6], above);
+}
+
 int main(int argc, char **argv) {
   const long long count = argc > 1 ? atoll(argv[1]) : (1ll << 28);
   const unsigned long long seed = argc > 2 ? strtoull(argv[2], nullptr, 10) : 1;
-  unsigned long long *bad = nullptr, h[5] = {0, 0, 0, 0, 0};
-  if (cudaMalloc(&bad, 5 * sizeof(unsigned long long)) != cudaSuccess) return 2;
-  cudaMemset(bad, 0, 5 * sizeof(unsigned long long));
+  unsigned long long *bad = nullptr, h[7] = {0, 0, 0, 0, 0, 0, 0};
+  if (cudaMalloc(&bad, sizeof(h)) != cudaSuccess) return 2;
+  cudaMemset(bad, 0, sizeof(h));
   check<<<152 * 8, 256>>>(count, seed, bad);
   check_lap<<<152 * 8, 256>>>(count / 4, seed, bad);
+  check_quot<<<152 * 8, 256>>>(count / 4, seed, bad);
   if (cudaMemcpy(h, bad, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) return 2;
-  printf("mismatches mul %llu add %llu to_float %llu of %lld; lap %llu of %lld (integer path %llu)\n", h[0], h[1],
-         h[2], count, h[3], count / 4, h[4]);
+  printf("mismatches mul %llu add %llu to_float %llu of %lld; lap %llu of %lld (integer path %llu); "
+         "quotient %llu of %lld (exceeding %llu)\n",
+         h[0], h[1], h[2], count, h[3], count / 4, h[4], h[5], count / 4, h[6]);
   cudaFree(bad);
-  return (h[0] || h[1] || h[2] || h[3]) ? 1 : 0;
+  return (h[0] || h[1] || h[2] || h[3] || h[5]) ? 1 : 0;
 }
