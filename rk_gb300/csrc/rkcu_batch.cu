@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(kT, batch_threads_per_sm<kExact>() / kT) batch
           }
         }
         if (last) {
-          double emax = em.best;
+          double emax = em.value();
 #pragma unroll
           for (int off = 16; off > 0; off >>= 1)
             emax = fmax(emax, __shfl_xor_sync(0xffffffffu, emax, off));

@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(kGenThreads)
     ynew[i] = yn;
     em.add(err, yn, yo);
   }
-  double m = em.best;
+  double m = em.value();
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, off));
   if ((threadIdx.x & 31) == 0) s_wmax[threadIdx.x >> 5] = m;

@@ -410,7 +410,7 @@ __global__ void __launch_bounds__(kRing ? kRingThreads : kThreads, kRing ? 1 : p
         stage_last(g.p, g.k, g.j);
       }
     }
-    double emax = em.best;
+    double emax = em.value();
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) emax = fmax(emax, __shfl_xor_sync(0xffffffffu, emax, off));
     if (lane == 0) s_wmax[warp] = emax;

@@ -23,7 +23,9 @@
 // balance: the products pay in the plain kernel's exact mode (tableau
 // products) and the Laplacian pays everywhere; a general software sum does not
 // (its alignment and normalisation cost more issue slots than the FP64 pipe
-// time it frees).
+// time it frees).  And the exact comparison of two quotients a / d > c / e by
+// their 106-bit cross products (quotients_greater), which lets the error norm's
+// maximum be found without a division per candidate.
 #pragma once
 
 #include <cstdint>
@@ -224,22 +226,26 @@ SFP_HD uint64_t mul_hi64(uint64_t a, uint64_t b) {
 #endif
 }
 
-// Whether a / d > r holds exactly, for positive normal doubles given as bit
-// patterns, decided as a > r d with the 106-bit product of the significands in
-// integers: no division and no FP64 instruction.  Rounding to nearest is
-// monotonic, so a quotient that does not exceed r exactly cannot round above
-// it, and the caller divides only when this returns true.
-//   a = ma 2^(ea-1075), r d = mr md 2^(er+ed-2150):  a > r d  <=>  ma 2^t > mr md,
-//   t = ea + 1075 - er - ed, with ma 2^t in [2^(52+t), 2^(53+t)) and mr md in [2^104, 2^106).
-SFP_HD bool quotient_exceeds(uint64_t ba, uint64_t bd, uint64_t br) {
+// Whether a / d > c / e holds exactly, for positive normal doubles given as
+// bit patterns: a e > c d with both 106-bit products of the significands in
+// integers.  With t = (ea + ee) - (ec + ed) the products scale as ma me 2^t
+// against mc md, both in [2^104, 2^106), so |t| >= 2 decides by itself.
+SFP_HD bool quotients_greater(uint64_t ba, uint64_t bd, uint64_t bc, uint64_t be) {
   constexpr uint64_t kF = 0x000fffffffffffffull, kH = 0x0010000000000000ull;
-  const int t = static_cast<int>(ba >> 52) + 1075 - static_cast<int>(bd >> 52) - static_cast<int>(br >> 52);
-  if (t >= 54) return true;
-  if (t <= 51) return false;
-  const uint64_t ma = (ba & kF) | kH, md = (bd & kF) | kH, mr = (br & kF) | kH;
-  const uint64_t lhi = ma >> (64 - t), llo = ma << t;  // t is 52 or 53
-  const uint64_t phi = mul_hi64(mr, md), plo = mr * md;
-  return lhi > phi || (lhi == phi && llo > plo);
+  const int t = static_cast<int>(ba >> 52) + static_cast<int>(be >> 52) - static_cast<int>(bc >> 52) -
+                static_cast<int>(bd >> 52);
+  if (t >= 2) return true;
+  if (t <= -2) return false;
+  const uint64_t ma = (ba & kF) | kH, md = (bd & kF) | kH, mc = (bc & kF) | kH, me = (be & kF) | kH;
+  uint64_t h1 = mul_hi64(ma, me), l1 = ma * me, h2 = mul_hi64(mc, md), l2 = mc * md;
+  if (t == 1) {
+    h1 = (h1 << 1) | (l1 >> 63);
+    l1 <<= 1;
+  } else if (t == -1) {
+    h2 = (h2 << 1) | (l2 >> 63);
+    l2 <<= 1;
+  }
+  return h1 > h2 || (h1 == h2 && l1 > l2);
 }
 
 // s rounded to a multiple of 2^k (k = 1, 2), ties to an even multiple of 2^k:

@@ -1,5 +1,5 @@
 // Bit-exactness check of the software binary64 multiply/add, the same-binade
-// Laplacian and the exact quotient test (rkcu_softfp64.cuh) against the host's
+// Laplacian and the exact quotient comparison (rkcu_softfp64.cuh) against the host's
 // IEEE round-to-nearest arithmetic.  Compiled with
 // -ffp-contract=off.  Usage: softfp64_check <count> <seed>; prints mismatches.
 #include <cinttypes>
@@ -121,40 +121,38 @@ int main(int argc, char **argv) {
   }
   printf("lap mismatches %lld (fast path taken %lld of %lld)\n", bad_lap, taken, count);
 
-  // the exact quotient test a / d > r against the product and its FMA error
-  // term (r d = p + err exactly in this exponent range): random operands, r
-  // the rounded quotient and its neighbours, and exactly representable
-  // quotients (few-bit significands, a = r d) with their neighbours
-  long long bad_quot = 0, above = 0;
+  // the exact comparison of two quotients a / d > c / e against the products
+  // a e and c d and their FMA error terms: random operands, equal quotients
+  // (c, e the same multiple of a, d) and their neighbours, and quotients one
+  // rounding apart
+  long long bad_q2 = 0, greater = 0;
   for (long long i = 0; i < count; ++i) {
-    const uint64_t r0 = next(), r1 = next(), r2 = next();
+    const uint64_t r0 = next(), r1 = next(), r2 = next(), r3 = next();
     auto band = [](uint64_t q, int lo, int span) {
       return double_of((q & 0x000fffffffffffffull) | (static_cast<uint64_t>(1023 + lo + static_cast<int>((q >> 52) % span)) << 52));
     };
-    double a = band(r0, -300, 600), d = band(r1, -300, 600), r;
-    switch (r2 % 4) {
-      case 0: r = band(r2, -300, 600); break;
-      case 1: r = double_of(bits_of(a / d) + (static_cast<int64_t>((r2 >> 8) % 5) - 2)); break;
-      case 2: {  // a / d exactly representable
-        d = double_of(bits_of(d) & ~0x000000ffffffffffull);
-        r = double_of(bits_of(band(r2, -300, 600)) & ~0x000000ffffffffffull);
-        a = r * d;
-        r = double_of(bits_of(r) + (static_cast<int64_t>((r2 >> 8) % 3) - 1));
+    double a = band(r0, -250, 500), d = band(r1, -250, 500), c, e;
+    switch (r3 % 4) {
+      case 0: c = band(r2, -250, 500); e = band(r3, -250, 500); break;
+      case 1: {  // c / e == a / d exactly, then moved by up to one unit in c or e
+        a = double_of(bits_of(a) & ~0x00000000000fffffull);
+        d = double_of(bits_of(d) & ~0x00000000000fffffull);
+        const double k = double_of((static_cast<uint64_t>(1023 + static_cast<int>(r2 % 40) - 20) << 52) | ((r2 >> 8) & 0xffff00000000ull));
+        c = a * k;
+        e = d * k;
+        const int64_t nudge = static_cast<int64_t>((r3 >> 8) % 3) - 1;
+        if ((r3 >> 16) & 1) c = double_of(bits_of(c) + nudge); else e = double_of(bits_of(e) + nudge);
         break;
       }
-      default: {  // a next to a representable r d
-        d = double_of(bits_of(d) & ~0x000000ffffffffffull);
-        r = double_of(bits_of(band(r2, -300, 600)) & ~0x000000ffffffffffull);
-        a = double_of(bits_of(r * d) + (static_cast<int64_t>((r2 >> 8) % 3) - 1));
-        break;
-      }
+      case 2: c = a / d * band(r2, 0, 1); e = band(r2, 0, 1); break;  // c / e near a / d
+      default: c = double_of(bits_of(a / d) + (static_cast<int64_t>((r2 >> 8) % 5) - 2)); e = 1.0; break;
     }
-    const double p = r * d, err = std::fma(r, d, -p);
-    const bool want = a > p || (a == p && err < 0.0);
-    const bool got = rkcu::softfp::quotient_exceeds(bits_of(a), bits_of(d), bits_of(r));
-    above += want;
-    if (got != want && bad_quot++ < 5) printf("quotient %a / %a > %a: want %d got %d\n", a, d, r, want, got);
+    const double p1 = a * e, e1 = std::fma(a, e, -p1), p2 = c * d, e2 = std::fma(c, d, -p2);
+    const bool want = p1 > p2 || (p1 == p2 && e1 > e2);
+    const bool got = rkcu::softfp::quotients_greater(bits_of(a), bits_of(d), bits_of(c), bits_of(e));
+    greater += want;
+    if (got != want && bad_q2++ < 5) printf("quotients %a / %a > %a / %a: want %d got %d\n", a, d, c, e, want, got);
   }
-  printf("quotient mismatches %lld (exceeding %lld of %lld)\n", bad_quot, above, count);
-  return (bad_mul || bad_add || bad_cvt || bad_lap || bad_quot) ? 1 : 0;
+  printf("quotient comparison mismatches %lld (greater %lld of %lld)\n", bad_q2, greater, count);
+  return (bad_mul || bad_add || bad_cvt || bad_lap || bad_q2) ? 1 : 0;
 }

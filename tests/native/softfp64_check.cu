@@ -1,5 +1,5 @@
 // Device check of the software binary64 multiply/add, double -> float
-// rounding, the same-binade Laplacian and the exact quotient test
+// rounding, the same-binade Laplacian and the exact quotient comparison
 // (rkcu_softfp64.cuh) against the FP64 pipe's __dmul_rn/__dadd_rn/__fma_rn/
 // __double2float_rn on random and adversarial operands.  Usage: softfp64_check_gpu <count> <seed>; prints mismatches.
 #include <cstdio>
@@ -96,43 +96,51 @@ __global__ void check_lap(long long count, unsigned long long seed, unsigned lon
   atomicAdd(&bad[4], taken);
 }
 
-// the exact quotient test a / d > r against the product and its FMA error term
-// (r d = p + err exactly in this exponent range), on the device: random
-// operands, r the rounded quotient and its neighbours, exactly representable
-// quotients and their neighbours
+// the exact comparison of two quotients a / d > c / e against the products a e
+// and c d and their FMA error terms, on the device: random operands, equal
+// quotients (c, e the same multiple of a, d) moved by up to one unit, and
+// quotients one rounding apart
 __device__ double band(uint64_t q) {
-  return double_of((q & 0x000fffffffffffffull) | ((uint64_t)(1023 - 300 + (int)((q >> 52) % 600)) << 52));
+  return double_of((q & 0x000fffffffffffffull) | ((uint64_t)(1023 - 250 + (int)((q >> 52) % 500)) << 52));
 }
 
 __global__ void check_quot(long long count, unsigned long long seed, unsigned long long *bad) {
   const long long stride = (long long)gridDim.x * blockDim.x;
-  unsigned long long bq = 0, above = 0;
+  unsigned long long bq = 0, greater = 0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < count; i += stride) {
-    const uint64_t r0 = mix(seed + 3 * i + 11), r1 = mix(seed + 3 * i + 12), r2 = mix(seed + 3 * i + 13);
-    double a = band(r0), d = band(r1), r;
-    const uint64_t low40 = 0x000000ffffffffffull;
-    switch (r2 % 4) {
-      case 0: r = band(r2); break;
-      case 1: r = double_of(bits_of(__ddiv_rn(a, d)) + ((int64_t)((r2 >> 8) % 5) - 2)); break;
-      case 2:
-        d = double_of(bits_of(d) & ~low40);
-        r = double_of(bits_of(band(r2)) & ~low40);
-        a = __dmul_rn(r, d);
-        r = double_of(bits_of(r) + ((int64_t)((r2 >> 8) % 3) - 1));
+    const uint64_t r0 = mix(seed + 4 * i + 11), r1 = mix(seed + 4 * i + 12), r2 = mix(seed + 4 * i + 13),
+                   r3 = mix(seed + 4 * i + 14);
+    double a = band(r0), d = band(r1), c, e;
+    switch (r3 % 4) {
+      case 0:
+        c = band(r2);
+        e = band(r3);
         break;
+      case 1: {
+        a = double_of(bits_of(a) & ~0x00000000000fffffull);
+        d = double_of(bits_of(d) & ~0x00000000000fffffull);
+        const double k = double_of(((uint64_t)(1023 + (int)(r2 % 40) - 20) << 52) | ((r2 >> 8) & 0xffff00000000ull));
+        c = __dmul_rn(a, k);
+        e = __dmul_rn(d, k);
+        const int64_t nudge = (int64_t)((r3 >> 8) % 3) - 1;
+        if ((r3 >> 16) & 1)
+          c = double_of(bits_of(c) + nudge);
+        else
+          e = double_of(bits_of(e) + nudge);
+        break;
+      }
       default:
-        d = double_of(bits_of(d) & ~low40);
-        r = double_of(bits_of(band(r2)) & ~low40);
-        a = double_of(bits_of(__dmul_rn(r, d)) + ((int64_t)((r2 >> 8) % 3) - 1));
+        c = double_of(bits_of(__ddiv_rn(a, d)) + ((int64_t)((r2 >> 8) % 5) - 2));
+        e = 1.0;
         break;
     }
-    const double p = __dmul_rn(r, d), err = __fma_rn(r, d, -p);
-    const bool want = a > p || (a == p && err < 0.0);
-    above += want;
-    if (quotient_exceeds(bits_of(a), bits_of(d), bits_of(r)) != want) ++bq;
+    const double p1 = __dmul_rn(a, e), e1 = __fma_rn(a, e, -p1), p2 = __dmul_rn(c, d), e2 = __fma_rn(c, d, -p2);
+    const bool want = p1 > p2 || (p1 == p2 && e1 > e2);
+    greater += want;
+    if (quotients_greater(bits_of(a), bits_of(d), bits_of(c), bits_of(e)) != want) ++bq;
   }
   if (bq) atomicAdd(&bad[5], bq);
-  atomicAdd(&bad[6], above);
+  atomicAdd(&bad[6], greater);
 }
 
 int main(int argc, char **argv) {
@@ -146,7 +154,7 @@ int main(int argc, char **argv) {
   check_quot<<<152 * 8, 256>>>(count / 4, seed, bad);
   if (cudaMemcpy(h, bad, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess) return 2;
   printf("mismatches mul %llu add %llu to_float %llu of %lld; lap %llu of %lld (integer path %llu); "
-         "quotient %llu of %lld (exceeding %llu)\n",
+         "quotient comparison %llu of %lld (greater %llu)\n",
          h[0], h[1], h[2], count, h[3], count / 4, h[4], h[5], count / 4, h[6]);
   cudaFree(bad);
   return (h[0] || h[1] || h[2] || h[3] || h[5]) ? 1 : 0;
