@@ -70,8 +70,8 @@ def fp64_ops_per_comp(method, precision):
     BRUSS2D-MIX step loop, counted from the kernel.  Operations: a right-hand
     side costs 9.5 (exact: 6.5 sums + 3 products) / 7.5 (fused) per component,
     each nonzero tableau coefficient a product and a sum (exact) or one FMA,
-    the update one sum, the error norm a few divisions (its integer filters
-    leave one for each component that raises a thread's maximum).  On the FP64
+    the update one sum, the error norm one division per thread and step (its
+    maximum is kept as an undivided quotient).  On the FP64
     pipe: the Laplacian's four sums run on the integer pipe (exact integer
     arithmetic where the five values share a binade, which is nearly every
     point), so a right-hand side keeps 2.5 sums per component; in the exact
@@ -79,8 +79,8 @@ def fp64_ops_per_comp(method, precision):
     work 6.3 per right-hand side) while the tableau products run in software
     binary64 on the integer pipe; the fused mode keeps 3.3 per right-hand side
     and computes the first stage's two plain products in software (ncu: 53.7
-    FP64-pipe instructions per DOPRI5(4) component-step; exact: DADD 50.7,
-    DMUL 21.1, DFMA 0.8, 72.6 in all, plus compares).
+    FP64-pipe instructions per DOPRI5(4) component-step; exact: DADD 50.6,
+    DMUL 21.1, DFMA 0.4, 72.1 in all, plus compares).
     The mixed form evaluates F0 in double-float arithmetic (FP32 pairs, the
     Laplacian in integer fixed point) and keeps three FP64 sums per
     component-step: y + (h sum b F0) as two sums, and y1 + dY."""
@@ -96,9 +96,12 @@ def fp64_ops_per_comp(method, precision):
         ops = 9.5 * s + 2 * nz_a + (2 * nz_b - 1) + (2 * nz_bh - 1) + 1.5
         if precision == "exact-hwmul":
             return 5.5 * s + 2 * nz_a + (2 * nz_b - 1) + (2 * nz_bh - 1) + 1.5, ops
-        return 6.3 * s + nz_a + (nz_b - 1) + (nz_bh - 1) + 0.9, ops
+        return 6.3 * s + nz_a + (nz_b - 1) + (nz_bh - 1) + 0.5, ops
     ops = 7.5 * s + nz_a + nz_b + nz_bh + 1.5
     return 3.3 * s + nz_a + (nz_b - 1) + (nz_bh - 1) + 1.5, ops
+
+
+E2E_RUNS = 3
 
 
 def _peaks():
@@ -372,17 +375,23 @@ def run_ours(args):
         dist.barrier()
     torch.cuda.synchronize()
     lib = rk.load()
-    t = time.perf_counter()
-    rc = lib.rkcu_begin(solver._h, T0, TE, ctypes.c_void_p(pinned_in.data_ptr()), 0, TOL)
-    assert rc == 0, rc
-    solver.run(args.steps)
-    rc = lib.rkcu_get_y(solver._h, ctypes.c_void_p(pinned_out.data_ptr()), 0)
-    assert rc == 0, rc
-    e2e_s = time.perf_counter() - t
-    st2 = solver.query()
-    e2e_steps = st2["steps_acc"] + st2["steps_rej"]
-    e2e_s = _max_over_ranks(e2e_s, dist, dev)
-    e2e_value = ws * e2e_steps / e2e_s
+    # three runs from y0, the median reported: one run is a few tens of ms of
+    # host-clock timing, which a host hiccup on the shared machine can stretch
+    e2e_runs = []
+    for _ in range(E2E_RUNS):
+        launches_e0 = solver.launches
+        t = time.perf_counter()
+        rc = lib.rkcu_begin(solver._h, T0, TE, ctypes.c_void_p(pinned_in.data_ptr()), 0, TOL)
+        assert rc == 0, rc
+        solver.run(args.steps)
+        rc = lib.rkcu_get_y(solver._h, ctypes.c_void_p(pinned_out.data_ptr()), 0)
+        assert rc == 0, rc
+        e2e_s = time.perf_counter() - t
+        st2 = solver.query()
+        e2e_steps = st2["steps_acc"] + st2["steps_rej"]
+        e2e_s = _max_over_ranks(e2e_s, dist, dev)
+        e2e_runs.append((ws * e2e_steps / e2e_s, solver.launches - launches_e0))
+    e2e_value = sorted(v for v, _ in e2e_runs)[len(e2e_runs) // 2]
     dev_bytes = solver.device_bytes
     solver.close()
 
@@ -431,7 +440,9 @@ def run_ours(args):
                           "fp64_ops_per_component_step": alg_opc},
         "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": 8.0 * n / max(1, e2e_steps),
                 "d2h_bytes_per_step": 8.0 * n / max(1, e2e_steps),
-                "note": f"one C-ABI begin/advance/get_y of {e2e_steps} steps, pinned host y0 and y"},
+                "runs": [round(v, 1) for v, _ in e2e_runs], "launches_per_run": [l for _, l in e2e_runs],
+                "note": f"C-ABI begin/advance/get_y of {e2e_steps} steps from y0 with pinned host y0 and y, "
+                        f"the median of {E2E_RUNS} runs"},
         "gpu_launches": launches,
         "host_pow_steps": host_pow_steps,
         "clocks": clk,
