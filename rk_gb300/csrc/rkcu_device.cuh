@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "rkcu_errmax.cuh"
 #include "rkcu_pow.cuh"
 #include "rkcu_softfp64.cuh"
 
@@ -322,74 +323,6 @@ __device__ __forceinline__ bool grid_barrier(DevState *st, unsigned int nblocks,
   __syncthreads();
   return s_ok != 0;
 }
-
-// Per-thread maximum of |e| / max(|y_new|, |y_old|) (include/tools.h:280-288)
-// kept as a quotient num / den that is divided once, when it is read.  Rounding
-// to nearest is monotonic, so the largest exact quotient rounds to the largest
-// rounded one, which is what the reference's fmax chain keeps.  Two tests on
-// the integer pipe decide whether a component raises the maximum.  The high
-// word of a positive double, (exponent << 20) | top mantissa bits, is 2^20
-// (log2 x + 1023) to within 0.086 * 2^20 (from below), so hi(|e|) - hi(divisor)
-// estimates 2^20 log2(ratio) to within 0.086 * 2^20 either way; a component
-// whose estimate is more than kMargin below the key of the current maximum
-// cannot exceed it.  A component that passes is compared exactly
-// (softfp::quotients_greater: |e| den > num divisor with the 106-bit products in
-// integers) and, if larger, becomes the maximum without a division.  Zero or
-// subnormal divisors and numerators, infinities and NaNs, and a maximum that is
-// still zero or subnormal, take the division path, which stores its rounded
-// quotient over 1, so the result is the reference's (a zero divisor gives
-// 1.7E308, a NaN ratio is ignored by fmax).
-struct ErrMax {
-  static constexpr int kMargin = 1 << 19;  // 0.5 in log2 units
-  static constexpr long long kMinNormal = 0x0010000000000000LL;
-  static constexpr long long kInf = 0x7ff0000000000000LL;
-  static constexpr long long kOne = 0x3ff0000000000000LL;
-  double num = 0.0, den = 1.0;
-  long long num_bits = 0, den_bits = kOne;
-  int best_key = -0x40000000;
-
-  // the maximum, rounded once
-  __device__ __forceinline__ double value() const { return den_bits == kOne ? num : num / den; }
-
-  __device__ __forceinline__ void add(double e, double yn, double yo) {
-    const long long ae = __double_as_longlong(e) & 0x7fffffffffffffffLL;
-    const long long an = __double_as_longlong(yn) & 0x7fffffffffffffffLL;
-    const long long ao = __double_as_longlong(yo) & 0x7fffffffffffffffLL;
-    const long long d = an > ao ? an : ao;
-    // a subnormal or zero divisor would make the estimate too low: exact path
-    const bool special = ae >= kInf || an > kInf || ao > kInf || d < kMinNormal;
-    const int key = static_cast<int>(ae >> 32) - static_cast<int>(d >> 32);
-    if (special) {
-      update(e, yn, yo);
-    } else if (key > best_key - kMargin) {
-      if (ae < kMinNormal || num_bits < kMinNormal) {
-        update(e, yn, yo);  // |e| zero or subnormal, or a maximum that is
-      } else if (num_bits < kInf &&
-                 softfp::quotients_greater(static_cast<uint64_t>(ae), static_cast<uint64_t>(d),
-                                           static_cast<uint64_t>(num_bits), static_cast<uint64_t>(den_bits))) {
-        num = __longlong_as_double(ae);
-        den = __longlong_as_double(d);
-        num_bits = ae;
-        den_bits = d;
-        best_key = key;
-      }
-    }
-  }
-
-  // the division path, kept out of line so that the division is not
-  // if-converted (run for every lane) by the compiler
-  __device__ __noinline__ void update(double e, double yn, double yo) {
-    const double div = fmax(fabs(yn), fabs(yo));
-    const double r = div == 0.0 ? 1.7E308 : fabs(e) / div;
-    if (r > value()) {  // false for NaN, as fmax would ignore it
-      num = r;
-      den = 1.0;
-      num_bits = __double_as_longlong(r);
-      den_bits = kOne;
-      best_key = static_cast<int>(num_bits >> 32) - 0x3ff00000;
-    }
-  }
-};
 
 // Neighbour synchronisation for the plain step loop: each CTA publishes how
 // many stages it has completed in this launch; a CTA starts a stage once the

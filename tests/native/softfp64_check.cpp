@@ -1,6 +1,7 @@
 // Bit-exactness check of the software binary64 multiply/add, the same-binade
 // Laplacian and the exact quotient comparison (rkcu_softfp64.cuh) against the host's
-// IEEE round-to-nearest arithmetic.  Compiled with
+// IEEE round-to-nearest arithmetic, and the error norm's maximum built on them
+// (rkcu_errmax.cuh) against the fmax chain it replaces.  Compiled with
 // -ffp-contract=off.  Usage: softfp64_check <count> <seed>; prints mismatches.
 #include <cinttypes>
 #include <cmath>
@@ -8,6 +9,7 @@
 #include <cstdlib>
 #include <cstring>
 
+#include "rkcu_errmax.cuh"
 #include "rkcu_softfp64.cuh"
 
 using rkcu::softfp::add;
@@ -154,5 +156,44 @@ int main(int argc, char **argv) {
     if (got != want && bad_q2++ < 5) printf("quotients %a / %a > %a / %a: want %d got %d\n", a, d, c, e, want, got);
   }
   printf("quotient comparison mismatches %lld (greater %lld of %lld)\n", bad_q2, greater, count);
-  return (bad_mul || bad_add || bad_cvt || bad_lap || bad_q2) ? 1 : 0;
+
+  // the error norm's maximum (ErrMax) against the fmax chain of rounded
+  // quotients, a zero divisor counting as 1.7E308: sequences of up to 64
+  // components of smooth fields (quotients within a few binades, many close
+  // to the maximum) mixed with zeros, subnormals, infinities and NaNs
+  long long bad_em = 0;
+  const long long seqs = count / 16;
+  for (long long i = 0; i < seqs; ++i) {
+    const uint64_t r = next();
+    const int len = 1 + static_cast<int>(r % 64);
+    const int special_rate = static_cast<int>((r >> 8) % 4);  // 0: none ... 3: often
+    const int spread = static_cast<int>((r >> 16) % 6);      // binades of the quotients
+    rkcu::ErrMax em;
+    double want = 0.0;
+    for (int k = 0; k < len; ++k) {
+      const uint64_t q = next(), q2 = next();
+      auto pick = [&](uint64_t z, int base) {
+        if (special_rate && (z >> 40) % (16 >> special_rate) == 0) {
+          switch ((z >> 50) % 6) {
+            case 0: return 0.0;
+            case 1: return double_of(z & 0x000fffffffffffffull);            // subnormal
+            case 2: return double_of(0x7ff0000000000000ull);                // infinity
+            case 3: return double_of(0x7ff8000000000000ull | (z & 0xffff)); // NaN
+            case 4: return double_of((z & 0x000fffffffffffffull) | 0x0010000000000000ull);  // smallest binade
+            default: return double_of((z & 0x000fffffffffffffull) | (2046ull << 52));       // largest binade
+          }
+        }
+        const int ex = base + static_cast<int>((z >> 52) % (spread + 1));
+        return double_of((z & 0x800fffffffffffffull) | (static_cast<uint64_t>(1023 + ex) << 52));
+      };
+      const double e = pick(q, -30), yn = pick(q2, 0), yo = (q2 >> 39) & 1 ? pick(next(), 0) : yn;
+      const double div = std::fmax(std::fabs(yn), std::fabs(yo));
+      want = std::fmax(want, div == 0.0 ? 1.7E308 : std::fabs(e) / div);
+      em.add(e, yn, yo);
+    }
+    const double got = em.value();
+    if (bits_of(got) != bits_of(want) && bad_em++ < 5) printf("error max of %d: want %a got %a\n", len, want, got);
+  }
+  printf("error max mismatches %lld of %lld sequences\n", bad_em, seqs);
+  return (bad_mul || bad_add || bad_cvt || bad_lap || bad_q2 || bad_em) ? 1 : 0;
 }
