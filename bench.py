@@ -55,7 +55,8 @@ FP64_PER_SM_CLK = 2.0
 # (dram__bytes_read.sum + dram__bytes_write.sum) at N=2000, DOPRI5(4); all
 # vectors exceed L2 at that size and above, so the figure scales with n.
 MEASURED_TRAFFIC = {
-    ("d", "exact", "DOPRI54"): (584.0, "one-pass ncu capture of the 61 timed launches of this benchmark's default command"),
+    ("d", "exact", "DOPRI54"): (584.0, "one-pass ncu capture (dram bytes and duration) of every plain_kernel launch "
+                                        "of this benchmark's default headline command: 583.9 B over the 20 timed steps"),
     ("d", "fma", "DOPRI54"): (573.0, "ncu --set full of a 3-step launch at N=2000"),
     ("d", "mixed", "DOPRI54"): (46.9, "ncu --set full of a 3-step launch at N=2000 (fused FP32 stages), scaled by n"),
 }
