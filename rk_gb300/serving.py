@@ -31,18 +31,19 @@ def make_request_problem(req):
 
 class ServingLoop:
     """sweeps_per_launch > 0 fixes the sweeps per launch; 0 chooses them per
-    launch as a time slice of about slice_s (a power of two, 1 .. max_sweeps)."""
+    launch as a time slice of about slice_s (a power of two, 1 .. max_sweeps).
+    `batch` serves through an existing object with rk_gb300.Batch's add / run /
+    finished / take / tune methods instead of a new Batch."""
 
     def __init__(self, arena_bytes, max_instances=4096, sweeps_per_launch=0, precision="exact",
-                 method="DOPRI54", device=0, stream=None, slice_s=0.004, max_sweeps=64):
-        self.batch = rk.Batch(arena_bytes, max_instances, method=method, precision=precision,
-                              device=device, stream=stream)
+                 method="DOPRI54", device=0, stream=None, slice_s=0.004, max_sweeps=64, batch=None):
+        self.batch = batch if batch is not None else rk.Batch(
+            arena_bytes, max_instances, method=method, precision=precision, device=device, stream=stream)
         self.fixed = sweeps_per_launch
         self.sweeps = sweeps_per_launch if sweeps_per_launch > 0 else 4
         self.slice_s = slice_s
         self.max_sweeps = max_sweeps
         self.sweep_s = None               # running estimate of one sweep's time
-        self.stages = rk.builtin_method(method)["s"]
 
     def _run_slice(self):
         """One launch; updates the per-sweep time estimate and the next sweep count."""
