@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "rkcu.h"
+#include "rkcu_arena.h"
 #include "rkcu_batch.cuh"
 
 using rkcu::BatchParams;
@@ -21,10 +22,6 @@ using rkcu::kMaxStages;
 namespace {
 
 constexpr size_t kAlign = 256;
-
-struct FreeBlock {
-  size_t off, size;
-};
 
 struct SlotInfo {
   int state = 0;  // 0 free, 1 active, 2 finished (result not taken yet)
@@ -59,7 +56,7 @@ struct rkcu_batch {
   rkcu::PowBox *d_box = nullptr;  // its device address
   char *arena = nullptr;
   size_t arena_bytes = 0;
-  std::vector<FreeBlock> free_list;
+  rkcu::ArenaList free_list;  // free byte ranges of the arena
   std::vector<SlotInfo> slots;
   int nslots_high = 0;
   std::vector<int> finished;
@@ -87,37 +84,6 @@ int fail(rkcu_batch *b, cudaError_t e, const char *what) {
     cudaError_t e_ = (call);                       \
     if (e_ != cudaSuccess) return fail(b, e_, #call); \
   } while (0)
-
-bool arena_alloc(rkcu_batch *b, size_t size, size_t *off) {
-  for (size_t i = 0; i < b->free_list.size(); ++i) {
-    FreeBlock &f = b->free_list[i];
-    if (f.size >= size) {
-      *off = f.off;
-      f.off += size;
-      f.size -= size;
-      if (f.size == 0) b->free_list.erase(b->free_list.begin() + i);
-      return true;
-    }
-  }
-  return false;
-}
-
-void arena_free(rkcu_batch *b, size_t off, size_t size) {
-  auto &fl = b->free_list;
-  auto it = std::lower_bound(fl.begin(), fl.end(), off,
-                             [](const FreeBlock &f, size_t o) { return f.off < o; });
-  it = fl.insert(it, FreeBlock{off, size});
-  // coalesce with the next and the previous block
-  size_t i = it - fl.begin();
-  if (i + 1 < fl.size() && fl[i].off + fl[i].size == fl[i + 1].off) {
-    fl[i].size += fl[i + 1].size;
-    fl.erase(fl.begin() + i + 1);
-  }
-  if (i > 0 && fl[i - 1].off + fl[i - 1].size == fl[i].off) {
-    fl[i - 1].size += fl[i].size;
-    fl.erase(fl.begin() + i);
-  }
-}
 
 BatchParams make_params(rkcu_batch *b) {
   BatchParams p;
@@ -317,7 +283,7 @@ int rkcu_batch_create(rkcu_batch **out, long long arena_bytes, int max_instances
   }
   b->arena_bytes = align_up((size_t)arena_bytes);
   if ((e = cudaMalloc(&b->arena, b->arena_bytes)) != cudaSuccess) return bail(fail(b, e, "arena"));
-  b->free_list.push_back(FreeBlock{0, b->arena_bytes});
+  b->free_list.reset(b->arena_bytes);
   if ((e = cudaMalloc(&b->d_desc, sizeof(InstDesc) * max_instances)) != cudaSuccess)
     return bail(fail(b, e, "desc"));
   if ((e = cudaMemset(b->d_desc, 0, sizeof(InstDesc) * max_instances)) != cudaSuccess)
@@ -381,7 +347,7 @@ int rkcu_batch_add(rkcu_batch *b, const rkcu_problem *prob, double t0, double te
   if (slot < 0) return RKCU_ERR_NOMEM;  // no free slot: admission refused
   const long long fp = rkcu_batch_footprint(prob, b->s);
   size_t off = 0;
-  if (fp < 0 || !arena_alloc(b, (size_t)fp, &off)) return RKCU_ERR_NOMEM;  // does not fit in HBM now
+  if (fp < 0 || !b->free_list.alloc((size_t)fp, &off)) return RKCU_ERR_NOMEM;  // does not fit in HBM now
   BCK(cudaSetDevice(b->opt.device));
   const size_t np = ((size_t)prob->n + 1) / 2;
   double2 *vec = reinterpret_cast<double2 *>(b->arena + off);
@@ -501,7 +467,7 @@ int rkcu_batch_take(rkcu_batch *b, int slot, double *y, rkcu_stats *stats, long 
     stats->host_pow_steps = si.host_pow;
   }
   if (host_id) *host_id = si.host_id;
-  arena_free(b, si.off, si.size);
+  b->free_list.release(si.off, si.size);
   si = SlotInfo();
   return RKCU_OK;
 }
@@ -585,9 +551,7 @@ int rkcu_batch_info(rkcu_batch *b, int *active, long long *free_bytes, long long
   if (!b) return RKCU_ERR_INVALID;
   if (active) *active = b->active;
   if (free_bytes) {
-    long long fb = 0;
-    for (auto &f : b->free_list) fb += (long long)f.size;
-    *free_bytes = fb;
+    *free_bytes = (long long)b->free_list.free_bytes();
   }
   if (launches) *launches = b->launches;
   return RKCU_OK;
